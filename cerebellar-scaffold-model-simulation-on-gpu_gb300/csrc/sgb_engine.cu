@@ -1,0 +1,858 @@
+// Simulation engine: builds the device layout from host networks, owns the
+// device memory, and drives the step kernels (see sgb_engine.h).
+//
+// The reference's equivalents are Initialization (GPUScaffoldSimulation.cu:
+// 132-631: population split, ELL upload, Philox state setup, streams) and
+// loop_n_steps (:693-791: per-ms launches on 12 streams + a device-wide
+// synchronize).  Here one handle holds any number of independent instances;
+// a chunk of steps is captured once as a CUDA graph whose step index lives in
+// device memory, so the same executable graph is replayed for every chunk.
+#include "sgb_engine.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+#include <numeric>
+#include <string>
+
+#include "sgb_philox.h"
+
+namespace sgb {
+
+#define SGB_CUDA(call)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return set_error(SGB_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                       __FILE__, __LINE__);                                                   \
+  } while (0)
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+Sim::~Sim() {
+  for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+  if (d_pool) cudaFree(d_pool);
+  if (d_misc) cudaFree(d_misc);
+  if (h_counts) cudaFreeHost(h_counts);
+  if (h_raster) cudaFreeHost(h_raster);
+  if (h_raster_off) cudaFreeHost(h_raster_off);
+  if (own_stream) cudaStreamDestroy(own_stream);
+}
+
+// ---------------------------------------------------------------------------
+// Per-segment LIF constants, folded once in double and rounded to float.
+static void fill_lif(SegDev& d, const Population& p, double dt, int substeps) {
+  d.El = p.El;
+  d.Vr = p.Vr;
+  d.Vth = p.Vth;
+  d.Ie = p.Ie;
+  d.neg_gL = -p.gL;
+  d.dt_cm = (float)(dt / (double)p.Cm);
+  // Reference: ref_step = (int)(target.dt_ref / DT) with DT a double literal
+  // (Simulation_header.cu:322).
+  d.ref_steps = (int32_t)((double)p.dt_ref / dt);
+  d.substeps = substeps;
+  for (int c = 0; c < 2; ++c) {
+    if (c < p.c_num) {
+      d.keep[c] = (float)(1.0 - dt / (double)p.tau[c]);
+      d.gw[c] = p.gbar[c] * p.w[c];
+      d.E[c] = p.E[c];
+      // Channel c integrates dg_exc when E_c > E_L, else dg_inh
+      // (Simulation_header.cu:347).
+      d.sel[c] = p.E[c] > p.El ? 0u : 1u;
+    } else {
+      d.keep[c] = 0.f;
+      d.gw[c] = 0.f;
+      d.E[c] = 0.f;
+      d.sel[c] = 0u;
+    }
+  }
+}
+
+static uint64_t poisson_threshold(float rate_hz, double dt_ms) {
+  const double p = (double)rate_hz * dt_ms / 1000.0;
+  if (!(p > 0.0)) return 0;
+  if (p >= 1.0) return 1ull << 32;
+  return (uint64_t)floor(p * 4294967296.0);
+}
+
+static void fill_source(SrcDev& d, const sgb_input_params& p, double dt_ms) {
+  memset(&d, 0, sizeof d);
+  d.kind = (uint32_t)p.kind;
+  d.thresh = p.kind == SGB_INPUT_POISSON ? poisson_threshold(p.rate_hz, dt_ms) : 0;
+  d.cyc = p.kind == SGB_INPUT_PERIODIC ? dt_ms * (double)p.rate_hz / 1000.0 : 0.0;
+  d.k_phase = llround(p.phase_ms / dt_ms);
+  d.win_period = p.win_period_ms > 0 ? llround(p.win_period_ms / dt_ms) : 0;
+  d.win_start = llround(p.win_start_ms / dt_ms);
+  d.win_end = llround(p.win_end_ms / dt_ms);
+  if (d.win_end <= d.win_start) d.win_start = d.win_end = 0;
+}
+
+// Initial potential of a LIF cell: Vr + (Vth - Vr) * U(0,1] (InitParams,
+// init_params.cu:346), U from Philox(seed; neuron, step 0, tag InitU).
+static float initial_u(const Population& p, uint64_t seed, uint32_t key) {
+  const U4 r = philox_draw(seed, key, 0, kTagInitU, 0);
+  return fmaf(p.Vth - p.Vr, u01_open0(r.x), p.Vr);
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+
+struct HostTables {
+  std::vector<uint32_t> csr_row, csr_syn, ell_syn;
+  std::vector<float> csr_wf, ell_wf;
+  std::vector<uint16_t> csr_wh, ell_wh;
+};
+
+void build_tables(const Projection& pr, int32_t npre, int32_t npost, bool bf16, ProjTables& t,
+                  HostTables& h) {
+  const size_t nnz = pr.pre_idx.size();
+  t.nnz = (int64_t)nnz;
+  // Pre-major CSR, synapses of a row in stored order.
+  h.csr_row.assign((size_t)npre + 1, 0);
+  for (size_t i = 0; i < nnz; ++i) h.csr_row[pr.pre_idx[i] + 1]++;
+  int32_t mx = 0;
+  for (int32_t j = 0; j < npre; ++j) {
+    mx = std::max<int32_t>(mx, (int32_t)h.csr_row[j + 1]);
+    h.csr_row[j + 1] += h.csr_row[j];
+  }
+  t.max_out = mx;
+  h.csr_syn.resize(nnz);
+  if (bf16) h.csr_wh.resize(nnz); else h.csr_wf.resize(nnz);
+  {
+    std::vector<uint32_t> fill(h.csr_row.begin(), h.csr_row.end() - 1);
+    for (size_t i = 0; i < nnz; ++i) {
+      const uint32_t q = fill[pr.pre_idx[i]]++;
+      h.csr_syn[q] = syn_pack(pr.post_idx[i], pr.delay[i]);
+      if (bf16) h.csr_wh[q] = f32_to_bf16_bits(pr.weight[i]); else h.csr_wf[q] = pr.weight[i];
+    }
+  }
+  // Post-major ELL, width = max in-degree, padding at the end of each row.
+  std::vector<uint32_t> indeg((size_t)npost, 0);
+  for (size_t i = 0; i < nnz; ++i) indeg[pr.post_idx[i]]++;
+  uint32_t K = 0;
+  for (uint32_t v : indeg) K = std::max(K, v);
+  t.ell_K = K;
+  t.ell_rowmajor = K > kEllColMajorMaxK;
+  const size_t cells = (size_t)K * (size_t)npost;
+  h.ell_syn.assign(cells, kEllPad);
+  if (bf16) h.ell_wh.assign(cells, 0); else h.ell_wf.assign(cells, 0.f);
+  std::vector<uint32_t> col((size_t)npost, 0);
+  for (size_t i = 0; i < nnz; ++i) {
+    const uint32_t p = pr.post_idx[i];
+    const uint32_t k = col[p]++;
+    const size_t q = t.ell_rowmajor ? (size_t)p * K + k : (size_t)k * npost + p;
+    h.ell_syn[q] = syn_pack(pr.pre_idx[i], pr.delay[i]);
+    if (bf16) h.ell_wh[q] = f32_to_bf16_bits(pr.weight[i]); else h.ell_wf[q] = pr.weight[i];
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+static int rebuild_work_lists(Sim& s, std::vector<PullTile>& tiles, std::vector<PullItem>& items) {
+  tiles.clear();
+  items.clear();
+  for (uint32_t pid = 0; pid < s.projs.size(); ++pid) {
+    const ProjDev& P = s.projs[pid];
+    if (P.mode != SGB_PROP_ELL || P.ell_K == 0) continue;
+    if (!P.ell_rowmajor) {
+      for (uint32_t p0 = 0; p0 < P.post_count; p0 += kPullThreadTile) tiles.push_back({pid, p0});
+    } else {
+      for (uint32_t p = 0; p < P.post_count; ++p)
+        for (uint32_t k0 = 0; k0 < P.ell_K; k0 += kPullWarpChunk) items.push_back({pid, p, k0});
+    }
+  }
+  return SGB_OK;
+}
+
+struct MiscLayout {
+  size_t ctl, segs, projs, srcs, out_list, seg_of_word, src_mask, outdeg, upd_tiles, pull_tiles,
+      pull_items, state, ring, hist, active, counts, raster, raster_off, totals, total;
+};
+
+int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seeds, int32_t n,
+               Sim** out) {
+  if (!out) return set_error(SGB_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  if (n < 1 || !nets) return set_error(SGB_ERR_ARG, "need at least one network");
+  if (!(cfg.dt_ms > 0.0)) return set_error(SGB_ERR_ARG, "dt_ms must be positive");
+  if (cfg.substeps < 1 || cfg.substeps > 1024)
+    return set_error(SGB_ERR_ARG, "substeps %d not in 1..1024", cfg.substeps);
+  if (cfg.chunk_steps < 1 || cfg.chunk_steps > 100000)
+    return set_error(SGB_ERR_ARG, "chunk_steps %d not in 1..100000", cfg.chunk_steps);
+  if (cfg.weight_type != SGB_WEIGHT_FP32 && cfg.weight_type != SGB_WEIGHT_BF16)
+    return set_error(SGB_ERR_ARG, "unknown weight type %d", cfg.weight_type);
+  if (cfg.exec_mode < SGB_EXEC_GRAPH || cfg.exec_mode > SGB_EXEC_STREAM)
+    return set_error(SGB_ERR_ARG, "unknown exec mode %d", cfg.exec_mode);
+  if (cfg.exec_mode == SGB_EXEC_PERSISTENT)
+    return set_error(SGB_ERR_UNSUPPORTED, "persistent execution is not available in this build");
+  if (cfg.default_prop != SGB_PROP_AUTO && cfg.default_prop != SGB_PROP_CSR &&
+      cfg.default_prop != SGB_PROP_ELL)
+    return set_error(SGB_ERR_ARG, "unknown default propagation mode %d", cfg.default_prop);
+  for (int32_t i = 0; i < n; ++i)
+    if (!nets[i]) return set_error(SGB_ERR_ARG, "network %d is NULL", i);
+
+  SGB_CUDA(cudaSetDevice(cfg.device));
+  std::unique_ptr<Sim> S(new Sim());
+  Sim& s = *S;
+  s.cfg = cfg;
+  s.bf16 = cfg.weight_type == SGB_WEIGHT_BF16;
+  s.chunk = (uint32_t)cfg.chunk_steps;
+  for (int32_t i = 0; i < n; ++i) {
+    s.nets.push_back(nets[i]->net);
+    s.seeds.push_back(seeds ? seeds[i] : (uint64_t)(i + 1));
+  }
+  int dev = cfg.device;
+  SGB_CUDA(cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, dev));
+  SGB_CUDA(cudaStreamCreateWithFlags(&s.own_stream, cudaStreamNonBlocking));
+  s.stream = s.own_stream;
+
+  // ---- segments -----------------------------------------------------------
+  uint64_t cursor = 0;
+  int64_t first_id = 0;
+  int max_delay = 1;
+  std::vector<std::vector<int32_t>> net_bits(n);
+  for (int32_t ni = 0; ni < n; ++ni) {
+    const Network& net = s.nets[ni];
+    s.net_seg0.push_back((int32_t)s.segs.size());
+    uint32_t key = 0;
+    accumulator_scale_bits(net, s.bf16, net_bits[ni]);
+    const std::vector<int32_t>& bits = net_bits[ni];
+    for (size_t pi = 0; pi < net.pops.size(); ++pi) {
+      const Population& p = net.pops[pi];
+      SegDev d;
+      memset(&d, 0, sizeof d);
+      cursor = align_up(cursor, 32);
+      d.base = (uint32_t)cursor;
+      d.count = (uint32_t)p.num;
+      d.key_base = key;
+      d.kind = p.dev_type == SGB_INPUT ? kSegInput : kSegLif;
+      d.seed = s.seeds[ni];
+      if (d.kind == kSegLif) fill_lif(d, p, cfg.dt_ms, cfg.substeps);
+      d.inv_scale[0] = ldexpf(1.0f, -bits[pi * 2 + 0]);
+      d.inv_scale[1] = ldexpf(1.0f, -bits[pi * 2 + 1]);
+      s.segs.push_back(d);
+      s.seg_first_id.push_back(first_id);
+      s.seg_net.push_back(ni);
+      s.seg_pop.push_back((int32_t)pi);
+      cursor += (uint64_t)p.num;
+      key += (uint32_t)p.num;
+      first_id += p.num;
+      if (cursor > 0xFFFFFF00ull) return set_error(SGB_ERR_UNSUPPORTED, "more than 2^32 cells");
+    }
+    for (const auto& pr : net.projs)
+      for (uint8_t d : pr.delay) max_delay = std::max(max_delay, (int)d);
+  }
+  if (s.segs.size() > 65535) return set_error(SGB_ERR_UNSUPPORTED, "more than 65535 segments");
+  s.n_pad = (uint32_t)align_up(std::max<uint64_t>(cursor, 32), 32);
+  s.n_words = s.n_pad / 32;
+  s.n_cells = first_id;
+  s.ring_slots = (uint32_t)max_delay + 1;
+  s.hist_rows = (uint32_t)max_delay;
+
+  // ---- sources ------------------------------------------------------------
+  std::vector<uint32_t> src_mask(s.n_pad, 0);
+  for (int32_t ni = 0; ni < n; ++ni) {
+    const Network& net = s.nets[ni];
+    s.net_src0.push_back((int32_t)s.srcs.size());
+    // Sources grouped by population so that each segment's are contiguous;
+    // within a net, sources keep their definition order.
+    for (size_t pi = 0; pi < net.pops.size(); ++pi) {
+      SegDev& d = s.segs[s.net_seg0[ni] + pi];
+      d.src_first = (uint32_t)s.srcs.size();
+      for (size_t si = 0; si < net.inputs.size(); ++si) {
+        const InputSource& src = net.inputs[si];
+        if (src.pop != (int32_t)pi) continue;
+        const uint32_t bit = (uint32_t)s.srcs.size() - d.src_first;
+        SrcDev sd;
+        fill_source(sd, src.p, cfg.dt_ms);
+        s.srcs.push_back(sd);
+        s.src_net.push_back(ni);
+        s.src_idx.push_back((int32_t)si);
+        for (uint32_t id : src.ids) src_mask[d.base + id] |= 1u << bit;
+      }
+      d.src_count = (uint32_t)s.srcs.size() - d.src_first;
+    }
+  }
+
+  // ---- projections and tables --------------------------------------------
+  std::vector<HostTables> host(0);
+  std::vector<std::vector<uint32_t>> seg_out(s.segs.size());
+  std::vector<uint32_t> outdeg(s.n_pad, 0);
+  size_t pool = 0;
+  const size_t wsz = s.bf16 ? 2 : 4;
+  for (int32_t ni = 0; ni < n; ++ni) {
+    const Network& net = s.nets[ni];
+    s.net_proj0.push_back((int32_t)s.projs.size());
+    const std::vector<int32_t>& bits = net_bits[ni];
+    for (size_t pj = 0; pj < net.projs.size(); ++pj) {
+      const Projection& pr = net.projs[pj];
+      ProjTables t;
+      t.net = ni;
+      t.proj = (int32_t)pj;
+      t.pre_seg = (uint32_t)(s.net_seg0[ni] + pr.pre);
+      t.post_seg = (uint32_t)(s.net_seg0[ni] + pr.post);
+      host.emplace_back();
+      build_tables(pr, net.pops[pr.pre].num, net.pops[pr.post].num, s.bf16, t, host.back());
+      const HostTables& h = host.back();
+      t.off_csr_row = pool; pool = align_up(pool + h.csr_row.size() * 4, 256);
+      t.off_csr_syn = pool; pool = align_up(pool + h.csr_syn.size() * 4, 256);
+      t.off_csr_w = pool; pool = align_up(pool + (size_t)t.nnz * wsz, 256);
+      t.off_ell_syn = pool; pool = align_up(pool + h.ell_syn.size() * 4, 256);
+      t.off_ell_w = pool; pool = align_up(pool + h.ell_syn.size() * wsz, 256);
+      ProjDev P;
+      memset(&P, 0, sizeof P);
+      const SegDev& pre = s.segs[t.pre_seg];
+      const SegDev& post = s.segs[t.post_seg];
+      P.pre_base = pre.base;
+      P.post_base = post.base;
+      P.pre_count = pre.count;
+      P.post_count = post.count;
+      P.channel = (uint32_t)pr.channel;
+      int mode = pr.mode == SGB_PROP_AUTO ? cfg.default_prop : pr.mode;
+      P.mode = (uint32_t)(mode == SGB_PROP_AUTO ? SGB_PROP_CSR : mode);
+      P.scale = ldexpf(1.0f, bits[pr.post * 2 + pr.channel]);
+      P.ell_K = t.ell_K;
+      P.ell_rowmajor = t.ell_rowmajor ? 1u : 0u;
+      seg_out[t.pre_seg].push_back((uint32_t)s.projs.size());
+      for (int32_t j = 0; j < pre.count; ++j)
+        outdeg[pre.base + j] += h.csr_row[j + 1] - h.csr_row[j];
+      s.n_syn += t.nnz;
+      s.projs.push_back(P);
+      s.ptab.push_back(t);
+    }
+  }
+  std::vector<uint32_t> out_list;
+  for (size_t si = 0; si < s.segs.size(); ++si) {
+    s.segs[si].out_first = (uint32_t)out_list.size();
+    s.segs[si].out_count = (uint32_t)seg_out[si].size();
+    out_list.insert(out_list.end(), seg_out[si].begin(), seg_out[si].end());
+  }
+  std::vector<uint16_t> seg_of_word(s.n_words, 0);
+  std::vector<UpdTile> upd;
+  for (size_t si = 0; si < s.segs.size(); ++si) {
+    const SegDev& d = s.segs[si];
+    for (uint32_t w = d.base / 32; w < (d.base + d.count + 31) / 32; ++w) seg_of_word[w] = (uint16_t)si;
+    for (uint32_t st = d.base; st < d.base + d.count; st += kUpdateTile) upd.push_back({(uint32_t)si, st});
+  }
+  std::vector<PullTile> ptiles;
+  std::vector<PullItem> pitems;
+  rebuild_work_lists(s, ptiles, pitems);
+  // Capacity for every projection in ELL mode, so modes can change later.
+  size_t cap_tiles = 0, cap_items = 0;
+  for (const ProjDev& P : s.projs) {
+    if (!P.ell_K) continue;
+    if (!P.ell_rowmajor) cap_tiles += (P.post_count + kPullThreadTile - 1) / kPullThreadTile;
+    else cap_items += (size_t)P.post_count * ((P.ell_K + kPullWarpChunk - 1) / kPullWarpChunk);
+  }
+
+  // ---- device memory -------------------------------------------------------
+  s.pool_bytes = std::max<size_t>(pool, 256);
+  SGB_CUDA(cudaMalloc(&s.d_pool, s.pool_bytes));
+  for (size_t i = 0; i < s.ptab.size(); ++i) {
+    const ProjTables& t = s.ptab[i];
+    const HostTables& h = host[i];
+    char* base = (char*)s.d_pool;
+    SGB_CUDA(cudaMemcpy(base + t.off_csr_row, h.csr_row.data(), h.csr_row.size() * 4, cudaMemcpyHostToDevice));
+    if (t.nnz) {
+      SGB_CUDA(cudaMemcpy(base + t.off_csr_syn, h.csr_syn.data(), h.csr_syn.size() * 4, cudaMemcpyHostToDevice));
+      SGB_CUDA(cudaMemcpy(base + t.off_csr_w, s.bf16 ? (const void*)h.csr_wh.data() : (const void*)h.csr_wf.data(),
+                          (size_t)t.nnz * wsz, cudaMemcpyHostToDevice));
+    }
+    if (!h.ell_syn.empty()) {
+      SGB_CUDA(cudaMemcpy(base + t.off_ell_syn, h.ell_syn.data(), h.ell_syn.size() * 4, cudaMemcpyHostToDevice));
+      SGB_CUDA(cudaMemcpy(base + t.off_ell_w, s.bf16 ? (const void*)h.ell_wh.data() : (const void*)h.ell_wf.data(),
+                          h.ell_syn.size() * wsz, cudaMemcpyHostToDevice));
+    }
+    ProjDev& P = s.projs[i];
+    P.csr_row = (const uint32_t*)(base + t.off_csr_row);
+    P.csr_syn = (const uint32_t*)(base + t.off_csr_syn);
+    P.csr_w = base + t.off_csr_w;
+    P.ell_syn = (const uint32_t*)(base + t.off_ell_syn);
+    P.ell_w = base + t.off_ell_w;
+  }
+  host.clear();
+  host.shrink_to_fit();
+
+  s.raster_cap = cfg.raster ? (uint32_t)std::min<uint64_t>((uint64_t)s.n_pad * s.chunk, 1ull << 24) : 0;
+  const size_t nseg = s.segs.size();
+  MiscLayout L;
+  size_t m = 0;
+  auto take = [&](size_t bytes) { size_t o = m; m = align_up(m + std::max<size_t>(bytes, 1), 256); return o; };
+  L.ctl = take(sizeof(Ctl));
+  L.segs = take(nseg * sizeof(SegDev));
+  L.projs = take(std::max<size_t>(s.projs.size(), 1) * sizeof(ProjDev));
+  L.srcs = take(std::max<size_t>(s.srcs.size(), 1) * sizeof(SrcDev));
+  L.out_list = take(std::max<size_t>(out_list.size(), 1) * 4);
+  L.seg_of_word = take((size_t)s.n_words * 2);
+  L.src_mask = take((size_t)s.n_pad * 4);
+  L.outdeg = take((size_t)s.n_pad * 4);
+  L.upd_tiles = take(std::max<size_t>(upd.size(), 1) * sizeof(UpdTile));
+  L.pull_tiles = take(std::max<size_t>(cap_tiles, 1) * sizeof(PullTile));
+  L.pull_items = take(std::max<size_t>(cap_items, 1) * sizeof(PullItem));
+  L.state = take((size_t)s.n_pad * sizeof(float4));
+  L.ring = take((size_t)s.ring_slots * s.n_pad * 8);
+  L.hist = take((size_t)s.hist_rows * s.n_words * 4);
+  L.active = take((size_t)2 * s.n_pad * 4);
+  L.counts = take((size_t)s.chunk * nseg * 4);
+  L.raster = take((size_t)std::max<uint32_t>(s.raster_cap, 1) * 4);
+  L.raster_off = take((size_t)(s.chunk + 1) * 4);
+  L.totals = take(nseg * sizeof(double));
+  L.total = m;
+  s.misc_bytes = m;
+  SGB_CUDA(cudaMalloc(&s.d_misc, s.misc_bytes));
+  SGB_CUDA(cudaMemset(s.d_misc, 0, s.misc_bytes));
+  char* mb = (char*)s.d_misc;
+
+  StepArgs& a = s.args;
+  memset(&a, 0, sizeof a);
+  a.ctl = (Ctl*)(mb + L.ctl);
+  a.segs = (const SegDev*)(mb + L.segs);
+  a.projs = (const ProjDev*)(mb + L.projs);
+  a.srcs = (const SrcDev*)(mb + L.srcs);
+  a.out_list = (const uint32_t*)(mb + L.out_list);
+  a.seg_of_word = (const uint16_t*)(mb + L.seg_of_word);
+  a.src_mask = (const uint32_t*)(mb + L.src_mask);
+  a.outdeg = (const uint32_t*)(mb + L.outdeg);
+  a.upd_tiles = (const UpdTile*)(mb + L.upd_tiles);
+  a.pull_tiles = (const PullTile*)(mb + L.pull_tiles);
+  a.pull_items = (const PullItem*)(mb + L.pull_items);
+  a.state = (float4*)(mb + L.state);
+  a.ring = (int*)(mb + L.ring);
+  a.hist = (uint32_t*)(mb + L.hist);
+  a.active = (uint32_t*)(mb + L.active);
+  a.counts = (uint32_t*)(mb + L.counts);
+  a.raster = (uint32_t*)(mb + L.raster);
+  a.raster_off = (uint32_t*)(mb + L.raster_off);
+  a.totals = (double*)(mb + L.totals);
+  a.n_pad = s.n_pad;
+  a.n_words = s.n_words;
+  a.n_segs = (uint32_t)nseg;
+  a.n_projs = (uint32_t)s.projs.size();
+  a.ring_slots = s.ring_slots;
+  a.hist_rows = s.hist_rows;
+  a.n_upd_tiles = (uint32_t)upd.size();
+  a.n_pull_tiles = (uint32_t)ptiles.size();
+  a.n_pull_items = (uint32_t)pitems.size();
+  a.raster_cap = s.raster_cap;
+  a.bf16 = s.bf16 ? 1 : 0;
+  a.substeps = cfg.substeps;
+  s.push_blocks = 2 * s.sm_count;
+
+  SGB_CUDA(cudaMemcpy((void*)a.segs, s.segs.data(), nseg * sizeof(SegDev), cudaMemcpyHostToDevice));
+  if (!s.projs.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
+  if (!s.srcs.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.srcs, s.srcs.data(), s.srcs.size() * sizeof(SrcDev), cudaMemcpyHostToDevice));
+  if (!out_list.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.out_list, out_list.data(), out_list.size() * 4, cudaMemcpyHostToDevice));
+  SGB_CUDA(cudaMemcpy((void*)a.seg_of_word, seg_of_word.data(), seg_of_word.size() * 2, cudaMemcpyHostToDevice));
+  SGB_CUDA(cudaMemcpy((void*)a.src_mask, src_mask.data(), src_mask.size() * 4, cudaMemcpyHostToDevice));
+  SGB_CUDA(cudaMemcpy((void*)a.outdeg, outdeg.data(), outdeg.size() * 4, cudaMemcpyHostToDevice));
+  if (!upd.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.upd_tiles, upd.data(), upd.size() * sizeof(UpdTile), cudaMemcpyHostToDevice));
+  if (!ptiles.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.pull_tiles, ptiles.data(), ptiles.size() * sizeof(PullTile), cudaMemcpyHostToDevice));
+  if (!pitems.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.pull_items, pitems.data(), pitems.size() * sizeof(PullItem), cudaMemcpyHostToDevice));
+
+  SGB_CUDA(cudaMallocHost(&s.h_counts, (size_t)s.chunk * nseg * 4));
+  SGB_CUDA(cudaMallocHost(&s.h_raster_off, (size_t)(s.chunk + 1) * 4));
+  if (s.raster_cap) SGB_CUDA(cudaMallocHost(&s.h_raster, (size_t)s.raster_cap * 4));
+
+  int rc = sim_reset(s, nullptr);
+  if (rc) return rc;
+  *out = S.release();
+  return SGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+int sim_reset(Sim& s, const uint64_t* seeds) {
+  if (seeds) {
+    for (size_t i = 0; i < s.nets.size(); ++i) s.seeds[i] = seeds[i];
+    for (size_t si = 0; si < s.segs.size(); ++si) s.segs[si].seed = s.seeds[s.seg_net[si]];
+    SGB_CUDA(cudaMemcpyAsync((void*)s.args.segs, s.segs.data(), s.segs.size() * sizeof(SegDev),
+                             cudaMemcpyHostToDevice, s.stream));
+  }
+  std::vector<float4> st(s.n_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+  for (size_t si = 0; si < s.segs.size(); ++si) {
+    const SegDev& d = s.segs[si];
+    if (d.kind != kSegLif) continue;
+    const Population& p = s.nets[s.seg_net[si]].pops[s.seg_pop[si]];
+    for (uint32_t j = 0; j < d.count; ++j)
+      st[d.base + j].x = initial_u(p, d.seed, d.key_base + j);
+  }
+  const StepArgs& a = s.args;
+  SGB_CUDA(cudaMemcpyAsync(a.state, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.ring, 0, (size_t)s.ring_slots * s.n_pad * 8, s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.hist, 0, (size_t)s.hist_rows * s.n_words * 4, s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.totals, 0, s.segs.size() * sizeof(double), s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  return SGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One chunk of c steps issued on `st` (direct launches; also the body that is
+// captured into a graph).
+static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nlaunch) {
+  const StepArgs& a = s.args;
+  cudaError_t e;
+  int64_t L = 0;
+  if ((e = cudaMemsetAsync(a.counts, 0, (size_t)c * a.n_segs * 4, st))) return e;
+  if ((e = launch_chunk_begin(a, st))) return e;
+  L++;
+  bool any_csr = false;
+  for (const ProjDev& P : s.projs) any_csr |= P.mode == SGB_PROP_CSR && P.pre_count && P.post_count;
+  for (uint32_t i = 0; i < c; ++i) {
+    if ((e = launch_update(a, st))) return e;
+    L += a.n_upd_tiles ? 1 : 0;
+    if (any_csr) {
+      if ((e = launch_push(a, s.push_blocks, st))) return e;
+      L++;
+    }
+    if ((e = launch_pull_thread(a, st))) return e;
+    L += a.n_pull_tiles ? 1 : 0;
+    if ((e = launch_pull_warp(a, st))) return e;
+    L += a.n_pull_items ? 1 : 0;
+    if ((e = launch_advance(a, st))) return e;
+    L++;
+  }
+  if ((e = launch_chunk_end(a, st))) return e;
+  L++;
+  if (nlaunch) *nlaunch = L;
+  return cudaSuccess;
+}
+
+static int get_graph(Sim& s, uint32_t c, cudaGraphExec_t* out, int64_t* nlaunch) {
+  auto it = s.graphs.find(c);
+  if (it != s.graphs.end()) {
+    // A graph launches the same kernels as the direct issue it was captured from.
+    bool any_csr = false;
+    for (const ProjDev& P : s.projs) any_csr |= P.mode == SGB_PROP_CSR && P.pre_count && P.post_count;
+    const StepArgs& a = s.args;
+    *out = it->second;
+    *nlaunch = 2 + (int64_t)c * ((a.n_upd_tiles ? 1 : 0) + (any_csr ? 1 : 0) +
+                                 (a.n_pull_tiles ? 1 : 0) + (a.n_pull_items ? 1 : 0) + 1);
+    return SGB_OK;
+  }
+  cudaGraph_t g;
+  SGB_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = issue_chunk(s, c, s.stream, nlaunch);
+  cudaError_t e2 = cudaStreamEndCapture(s.stream, &g);
+  if (e != cudaSuccess)
+    return set_error(SGB_ERR_CUDA, "capture of a %u-step chunk failed: %s", c, cudaGetErrorString(e));
+  if (e2 != cudaSuccess)
+    return set_error(SGB_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
+  cudaGraphExec_t ge;
+  e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_error(SGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  s.graphs[c] = ge;
+  *out = ge;
+  return SGB_OK;
+}
+
+static void drop_graphs(Sim& s) {
+  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
+  s.graphs.clear();
+}
+
+static int launch_chunk(Sim& s, uint32_t c) {
+  int64_t L = 0;
+  if (s.cfg.exec_mode == SGB_EXEC_GRAPH) {
+    cudaGraphExec_t ge;
+    int rc = get_graph(s, c, &ge, &L);
+    if (rc) return rc;
+    SGB_CUDA(cudaGraphLaunch(ge, s.stream));
+  } else {
+    cudaError_t e = issue_chunk(s, c, s.stream, &L);
+    if (e != cudaSuccess) return set_error(SGB_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
+  }
+  s.launches += L;
+  return SGB_OK;
+}
+
+static int check_device_error(Sim& s, uint32_t* bits) {
+  uint32_t err = 0;
+  SGB_CUDA(cudaMemcpyAsync(&err, &s.args.ctl->error, 4, cudaMemcpyDeviceToHost, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  if (bits) *bits = err;
+  return SGB_OK;
+}
+
+int sim_enqueue(Sim& s, int64_t n_steps) {
+  if (n_steps < 0) return set_error(SGB_ERR_ARG, "n_steps is negative");
+  for (int64_t done = 0; done < n_steps;) {
+    const uint32_t c = (uint32_t)std::min<int64_t>(s.chunk, n_steps - done);
+    int rc = launch_chunk(s, c);
+    if (rc) return rc;
+    done += c;
+  }
+  return SGB_OK;
+}
+
+int sim_sync(Sim& s) {
+  uint32_t err = 0;
+  int rc = check_device_error(s, &err);
+  if (rc) return rc;
+  SGB_CUDA(cudaMemsetAsync(&s.args.ctl->error, 0, 4, s.stream));
+  if (err & kErrBarrierTimeout) return set_error(SGB_ERR_DEVICE, "a device-side wait hit its limit");
+  return SGB_OK;
+}
+
+int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int64_t raster_cap,
+            int64_t* raster_offsets) {
+  if (n_steps < 0) return set_error(SGB_ERR_ARG, "n_steps is negative");
+  const bool want_raster = raster_ids || raster_offsets;
+  if (want_raster && !s.raster_cap)
+    return set_error(SGB_ERR_STATE, "raster output needs a handle created with cfg.raster = 1");
+  if (want_raster && (!raster_ids || !raster_offsets))
+    return set_error(SGB_ERR_ARG, "raster_ids and raster_offsets go together");
+  const size_t nseg = s.segs.size();
+  int64_t done = 0, rfill = 0;
+  bool overflow = false;
+  if (raster_offsets) raster_offsets[0] = 0;
+  while (done < n_steps) {
+    const uint32_t c = (uint32_t)std::min<int64_t>(s.chunk, n_steps - done);
+    int rc = launch_chunk(s, c);
+    if (rc) return rc;
+    if (counts || want_raster) {
+      const StepArgs& a = s.args;
+      SGB_CUDA(cudaMemcpyAsync(s.h_counts, a.counts, (size_t)c * nseg * 4, cudaMemcpyDeviceToHost, s.stream));
+      if (want_raster)
+        SGB_CUDA(cudaMemcpyAsync(s.h_raster_off, a.raster_off, (size_t)(c + 1) * 4, cudaMemcpyDeviceToHost, s.stream));
+      SGB_CUDA(cudaStreamSynchronize(s.stream));
+      if (counts) memcpy(counts + (size_t)done * nseg, s.h_counts, (size_t)c * nseg * 4);
+      if (want_raster) {
+        const uint32_t nrec = std::min<uint32_t>(s.h_raster_off[c], s.raster_cap);
+        if (nrec) {
+          SGB_CUDA(cudaMemcpyAsync(s.h_raster, a.raster, (size_t)nrec * 4, cudaMemcpyDeviceToHost, s.stream));
+          SGB_CUDA(cudaStreamSynchronize(s.stream));
+        }
+        for (uint32_t r = 0; r < c; ++r) {
+          const uint32_t b = s.h_raster_off[r], e = s.h_raster_off[r + 1];
+          const int64_t start = rfill;
+          for (uint32_t q = b; q < e; ++q) {
+            if (q >= s.raster_cap || rfill >= raster_cap) {
+              overflow = true;
+              break;
+            }
+            const uint32_t pid = s.h_raster[q];
+            // Segment of the padded id by binary search over bases.
+            size_t lo = 0, hi = nseg;
+            while (hi - lo > 1) {
+              const size_t mid = (lo + hi) / 2;
+              if (s.segs[mid].base <= pid) lo = mid; else hi = mid;
+            }
+            raster_ids[rfill++] = (uint32_t)(s.seg_first_id[lo] + (pid - s.segs[lo].base));
+          }
+          std::sort(raster_ids + start, raster_ids + rfill);
+          raster_offsets[done + r + 1] = rfill;
+        }
+      }
+    }
+    done += c;
+  }
+  uint32_t err = 0;
+  int rc = check_device_error(s, &err);
+  if (rc) return rc;
+  SGB_CUDA(cudaMemsetAsync(&s.args.ctl->error, 0, 4, s.stream));
+  if (err & kErrBarrierTimeout) return set_error(SGB_ERR_DEVICE, "a device-side wait hit its limit");
+  if (overflow || (want_raster && (err & kErrRasterOverflow)))
+    return set_error(SGB_ERR_OVERFLOW, "raster buffer too small; counts and state are intact");
+  return SGB_OK;
+}
+
+int sim_set_rates(Sim& s, int32_t net, int32_t n, const float* rates) {
+  if (net < 0 || net >= (int32_t)s.nets.size()) return set_error(SGB_ERR_ARG, "net %d out of range", net);
+  const int32_t nsrc = (int32_t)s.nets[net].inputs.size();
+  if (n != nsrc || (!rates && n)) return set_error(SGB_ERR_ARG, "net %d has %d sources, got %d rates", net, nsrc, n);
+  for (int32_t i = 0; i < n; ++i)
+    if (!(rates[i] >= 0.f)) return set_error(SGB_ERR_ARG, "rate %d must be >= 0", i);
+  for (size_t k = 0; k < s.srcs.size(); ++k) {
+    if (s.src_net[k] != net) continue;
+    sgb_input_params& p = s.nets[net].inputs[s.src_idx[k]].p;
+    p.rate_hz = rates[s.src_idx[k]];
+    fill_source(s.srcs[k], p, s.cfg.dt_ms);
+  }
+  if (!s.srcs.empty())
+    SGB_CUDA(cudaMemcpyAsync((void*)s.args.srcs, s.srcs.data(), s.srcs.size() * sizeof(SrcDev),
+                             cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  return SGB_OK;
+}
+
+int sim_get_state(Sim& s, float* u, float* g, int32_t* ref) {
+  std::vector<float4> st(s.n_pad);
+  SGB_CUDA(cudaMemcpyAsync(st.data(), s.args.state, st.size() * sizeof(float4), cudaMemcpyDeviceToHost, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  for (size_t si = 0; si < s.segs.size(); ++si) {
+    const SegDev& d = s.segs[si];
+    const int64_t f = s.seg_first_id[si];
+    for (uint32_t j = 0; j < d.count; ++j) {
+      const float4 v = st[d.base + j];
+      int32_t r;
+      memcpy(&r, &v.w, 4);
+      if (u) u[f + j] = v.x;
+      if (g) { g[2 * (f + j)] = v.y; g[2 * (f + j) + 1] = v.z; }
+      if (ref) ref[f + j] = r;
+    }
+  }
+  return SGB_OK;
+}
+
+int sim_set_state(Sim& s, const float* u, const float* g, const int32_t* ref) {
+  std::vector<float4> st(s.n_pad);
+  SGB_CUDA(cudaMemcpyAsync(st.data(), s.args.state, st.size() * sizeof(float4), cudaMemcpyDeviceToHost, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  for (size_t si = 0; si < s.segs.size(); ++si) {
+    const SegDev& d = s.segs[si];
+    if (d.kind != kSegLif) continue;
+    const int64_t f = s.seg_first_id[si];
+    for (uint32_t j = 0; j < d.count; ++j) {
+      float4& v = st[d.base + j];
+      if (u) v.x = u[f + j];
+      if (g) { v.y = g[2 * (f + j)]; v.z = g[2 * (f + j) + 1]; }
+      if (ref) {
+        if (ref[f + j] < 0) return set_error(SGB_ERR_ARG, "negative refractory count");
+        memcpy(&v.w, &ref[f + j], 4);
+      }
+    }
+  }
+  SGB_CUDA(cudaMemcpyAsync(s.args.state, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  return SGB_OK;
+}
+
+int sim_totals(Sim& s, double* totals) {
+  if (!totals) return set_error(SGB_ERR_ARG, "totals is NULL");
+  SGB_CUDA(cudaMemcpyAsync(totals, s.args.totals, s.segs.size() * sizeof(double), cudaMemcpyDeviceToHost, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  return SGB_OK;
+}
+
+static int upload_modes(Sim& s) {
+  std::vector<PullTile> tiles;
+  std::vector<PullItem> items;
+  rebuild_work_lists(s, tiles, items);
+  StepArgs& a = s.args;
+  SGB_CUDA(cudaMemcpyAsync((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice, s.stream));
+  if (!tiles.empty())
+    SGB_CUDA(cudaMemcpyAsync((void*)a.pull_tiles, tiles.data(), tiles.size() * sizeof(PullTile), cudaMemcpyHostToDevice, s.stream));
+  if (!items.empty())
+    SGB_CUDA(cudaMemcpyAsync((void*)a.pull_items, items.data(), items.size() * sizeof(PullItem), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  a.n_pull_tiles = (uint32_t)tiles.size();
+  a.n_pull_items = (uint32_t)items.size();
+  drop_graphs(s);
+  return SGB_OK;
+}
+
+int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
+  if (net < 0 || net >= (int32_t)s.nets.size()) return set_error(SGB_ERR_ARG, "net %d out of range", net);
+  if (proj < 0 || proj >= (int32_t)s.nets[net].projs.size())
+    return set_error(SGB_ERR_ARG, "projection %d out of range", proj);
+  if (mode != SGB_PROP_CSR && mode != SGB_PROP_ELL) return set_error(SGB_ERR_ARG, "mode must be CSR or ELL");
+  s.projs[s.net_proj0[net] + proj].mode = (uint32_t)mode;
+  return upload_modes(s);
+}
+
+int sim_set_stream(Sim& s, cudaStream_t st) {
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  s.stream = st ? st : s.own_stream;
+  return SGB_OK;
+}
+
+int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
+  (void)s; (void)n_steps; (void)cache_path;
+  return set_error(SGB_ERR_UNSUPPORTED, "autotuner not available in this build");
+}
+
+// Instrumented run: the step loop with plain launches, each kernel class
+// bracketed by CUDA events on the handle's stream, synchronised per step so
+// the per-step spike and delivery counters can be read.
+int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t* launches) {
+  if (n_steps < 1) return set_error(SGB_ERR_ARG, "n_steps must be >= 1");
+  constexpr int K = SGB_KCLASS_COUNT;
+  const StepArgs& a = s.args;
+  const double W = s.bf16 ? 2.0 : 4.0;
+  // Static bytes per launch: update and the two dense pulls.
+  double upd_bytes = (double)a.n_words * 4.0;
+  for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 40.0 * d.count : 4.0 * d.count;
+  double pt_bytes = 0, pw_bytes = 0;
+  for (const ProjDev& P : s.projs) {
+    if (P.mode != SGB_PROP_ELL || !P.ell_K) continue;
+    const double b = (double)P.post_count * P.ell_K * (4.0 + W) + (double)P.post_count * 8.0;
+    (P.ell_rowmajor ? pw_bytes : pt_bytes) += b;
+  }
+  bool any_csr = false;
+  for (const ProjDev& P : s.projs) any_csr |= P.mode == SGB_PROP_CSR && P.pre_count && P.post_count;
+  cudaEvent_t ev[2 * K];
+  for (auto& e : ev) SGB_CUDA(cudaEventCreate(&e));
+  double tot_ms[K] = {0}, tot_bytes[K] = {0};
+  int64_t nl[K] = {0};
+  Ctl before, after;
+  int32_t done = 0;
+  int rc = SGB_OK;
+  while (done < n_steps && rc == SGB_OK) {
+    const uint32_t c = (uint32_t)std::min<int64_t>(s.chunk, n_steps - done);
+    SGB_CUDA(cudaMemsetAsync(a.counts, 0, (size_t)c * a.n_segs * 4, s.stream));
+    SGB_CUDA(launch_chunk_begin(a, s.stream));
+    for (uint32_t i = 0; i < c; ++i) {
+      SGB_CUDA(cudaMemcpyAsync(&before, a.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream));
+      bool ran[K] = {false, false, false, false, false};
+      auto timed = [&](int k, cudaError_t (*fn)(const StepArgs&, cudaStream_t), bool on) -> cudaError_t {
+        if (!on) return cudaSuccess;
+        cudaEventRecord(ev[2 * k], s.stream);
+        cudaError_t e = fn(a, s.stream);
+        cudaEventRecord(ev[2 * k + 1], s.stream);
+        ran[k] = true;
+        return e;
+      };
+      cudaError_t e = timed(0, launch_update, a.n_upd_tiles > 0);
+      if (!e && any_csr) {
+        cudaEventRecord(ev[2], s.stream);
+        e = launch_push(a, s.push_blocks, s.stream);
+        cudaEventRecord(ev[3], s.stream);
+        ran[1] = true;
+      }
+      if (!e) e = timed(2, launch_pull_thread, a.n_pull_tiles > 0);
+      if (!e) e = timed(3, launch_pull_warp, a.n_pull_items > 0);
+      if (!e) e = timed(4, launch_advance, true);
+      if (e) return set_error(SGB_ERR_CUDA, "profiled launch failed: %s", cudaGetErrorString(e));
+      SGB_CUDA(cudaMemcpyAsync(&after, a.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream));
+      SGB_CUDA(cudaStreamSynchronize(s.stream));
+      const double spikes = (double)after.active_count[before.step & 1];
+      const double deliv = (double)(after.delivered - before.delivered);
+      const double step_bytes[K] = {upd_bytes + spikes * 4.0, deliv * (12.0 + W) + spikes * 12.0,
+                                    pt_bytes, pw_bytes, 64.0};
+      for (int k = 0; k < K; ++k) {
+        if (!ran[k]) continue;
+        float ms = 0.f;
+        SGB_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
+        tot_ms[k] += ms;
+        tot_bytes[k] += step_bytes[k];
+        nl[k]++;
+      }
+    }
+    SGB_CUDA(launch_chunk_end(a, s.stream));
+    s.launches += 2;
+    done += (int32_t)c;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  for (int k = 0; k < K; ++k) {
+    s.launches += nl[k];
+    if (mean_us) mean_us[k] = nl[k] ? 1000.0 * tot_ms[k] / (double)nl[k] : 0.0;
+    if (bytes) bytes[k] = nl[k] ? tot_bytes[k] / (double)nl[k] : 0.0;
+    if (launches) launches[k] = nl[k];
+  }
+  return rc;
+}
+
+}  // namespace sgb

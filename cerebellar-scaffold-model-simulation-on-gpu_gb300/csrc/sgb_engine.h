@@ -1,0 +1,92 @@
+// Simulation handle: device layout of every instance, synapse tables, step
+// drivers (CUDA graph / persistent kernel / plain launches) and host I/O.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <vector>
+
+#include "sgb_device.h"
+#include "sgb_model.h"
+
+namespace sgb {
+
+struct ProjTables {
+  int32_t net = 0, proj = 0;
+  uint32_t pre_seg = 0, post_seg = 0;
+  int64_t nnz = 0;
+  uint32_t ell_K = 0;
+  bool ell_rowmajor = false;
+  int32_t max_out = 0;
+  // Device sub-allocations inside the table pool.
+  size_t off_csr_row = 0, off_csr_syn = 0, off_csr_w = 0, off_ell_syn = 0, off_ell_w = 0;
+};
+
+struct Sim {
+  sgb_config cfg{};
+  std::vector<Network> nets;
+  std::vector<uint64_t> seeds;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  int sm_count = 0;
+
+  // Layout.
+  std::vector<SegDev> segs;
+  std::vector<int64_t> seg_first_id;  // global unpadded id of cell 0
+  std::vector<int32_t> seg_net, seg_pop;
+  std::vector<int32_t> net_seg0;      // first segment of each net
+  std::vector<int32_t> net_proj0;     // first projection of each net
+  std::vector<int32_t> net_src0;      // first source of each net (in srcs)
+  std::vector<ProjDev> projs;
+  std::vector<ProjTables> ptab;
+  std::vector<SrcDev> srcs;
+  std::vector<int32_t> src_net, src_idx;
+  uint32_t n_pad = 0, n_words = 0, ring_slots = 2, hist_rows = 1;
+  int64_t n_cells = 0, n_syn = 0;
+  uint32_t chunk = 1000, raster_cap = 0;
+  bool bf16 = false;
+
+  // Device memory.
+  void* d_pool = nullptr;   // synapse tables
+  size_t pool_bytes = 0;
+  void* d_misc = nullptr;   // everything else
+  size_t misc_bytes = 0;
+  StepArgs args{};
+  int push_blocks = 0;
+
+  // Host staging for outputs.
+  uint32_t* h_counts = nullptr;
+  uint32_t* h_raster = nullptr;
+  uint32_t* h_raster_off = nullptr;
+
+  std::map<uint32_t, cudaGraphExec_t> graphs;  // by chunk length
+  int64_t launches = 0;
+  int64_t launches_per_step = 0;
+
+  ~Sim();
+};
+
+int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seeds, int32_t n,
+               Sim** out);
+int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int64_t raster_cap,
+            int64_t* raster_offsets);
+int sim_reset(Sim& s, const uint64_t* seeds);
+int sim_enqueue(Sim& s, int64_t n_steps);
+int sim_sync(Sim& s);
+int sim_set_rates(Sim& s, int32_t net, int32_t n, const float* rates);
+int sim_get_state(Sim& s, float* u, float* g, int32_t* ref);
+int sim_set_state(Sim& s, const float* u, const float* g, const int32_t* ref);
+int sim_totals(Sim& s, double* totals);
+int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode);
+int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path);
+int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t* launches);
+int sim_set_stream(Sim& s, cudaStream_t st);
+
+// Network handle behind the C ABI.
+}  // namespace sgb
+
+struct sgb_net {
+  sgb::Network net;
+};
+struct sgb_sim {
+  sgb::Sim* sim;
+};
