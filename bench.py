@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark of the scaffold simulation hot path: realtime factor (RTF).
+
+One bench step = one chunk of 1,000 exchange steps of 0.1 ms (0.1 s of
+biological time) of the configured workload, replayed as one CUDA graph.
+Rank 0 prints one JSON line.  `--impl reference` times the reference's own
+CPU path (its compiled functions where built, else their C restatement) on
+the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cerebellar-scaffold-model-simulation-on-gpu_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "realtime factor (biological s per wall s), 100k-cell scaffold"
+WORKLOADS = {
+    "c2": dict(config=2, scale=1.0, instances=1, bf16=False,
+               desc="config 2: 92,550-cell scaffold, 2,731,520 synapses, FP32 weights, 1 instance"),
+    "c3": dict(config=2, scale=1.0, instances=1, bf16=True,
+               desc="config 3: config-2 scaffold with BF16 synapse weights, 1 instance"),
+    "c4": dict(config=2, scale=None, instances=64, bf16=True,
+               desc="config 4: 64 config-2 instances scaled U[0.25,2.0], BF16, batched"),
+    "c1": dict(config=1, scale=1.0, instances=1, bf16=False,
+               desc="config 1: 9,256-cell net, 196,960 synapses, FP32"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--chunk", type=int, default=1000, help="exchange steps per bench step")
+    ap.add_argument("--ref-sample", type=int, default=100,
+                    help="exchange steps per bench step of the reference arm")
+    ap.add_argument("--cpu-sample", type=int, default=1000,
+                    help="exchange steps of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def build_nets(wl: dict, rank: int):
+    import scaffold_gb300 as sg
+
+    n = wl["instances"]
+    seeds = [1 + rank * 1000 + k for k in range(n)]
+    scales = sg.batched_scales(seeds) if wl["scale"] is None else [wl["scale"]] * n
+    nets = [sg.scaffold(wl["config"], sc, sd) for sc, sd in zip(scales, seeds)]
+    return nets, seeds
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        for k in ("hbm_gbs", "hbm_GBs", "hbm_copy_gbs"):
+            if k in d and d[k]:
+                return float(d[k]), "measured"
+    except (OSError, ValueError):
+        pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def cpu_baseline(wl: dict, sample_steps: int):
+    """Reference CPU path on a bounded sample of the workload, all host threads."""
+    import oracle_py
+    import scaffold_gb300 as sg
+
+    net = sg.scaffold(wl["config"], wl["scale"] or 1.0, 1)
+    desc = oracle_py.describe(net)
+    threads = os.cpu_count() or 1
+    if oracle_py.have_ref_harness(1):
+        ref, kind = oracle_py.RefHarness(desc, seed=1, bf16=wl["bf16"]), "reference"
+    else:
+        ref, kind = oracle_py.RefPort(desc, seed=1, bf16=wl["bf16"]), "port"
+    ref.run(20, threads=threads)  # warm caches and thread pool
+    t0 = time.perf_counter()
+    ref.run(sample_steps, threads=threads)
+    dt = time.perf_counter() - t0
+    rtf = sample_steps * 0.1e-3 / dt
+    return {"value": rtf, "unit": "x realtime", "cores": threads, "kind": kind,
+            "sample": f"{sample_steps} exchange steps (0.1 ms) of {wl['desc']}; dense per-delay "
+                      f"ELL pull + LIF update as in host_spike_propagation/host_update_lif_ch, "
+                      f"OpenMP over post cells"}
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle_py
+    import scaffold_gb300 as sg
+
+    wl = WORKLOADS[a.workload]
+    net = sg.scaffold(wl["config"], wl["scale"] or 1.0, 1)
+    desc = oracle_py.describe(net)
+    threads = os.cpu_count() or 1
+    if oracle_py.have_ref_harness(1):
+        ref, kind = oracle_py.RefHarness(desc, seed=1, bf16=wl["bf16"]), "reference"
+    else:
+        ref, kind = oracle_py.RefPort(desc, seed=1, bf16=wl["bf16"]), "port"
+    for _ in range(a.warmup):
+        ref.run(a.ref_sample, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        ref.run(a.ref_sample, threads=threads)
+    dt = time.perf_counter() - t0
+    bio = a.steps * a.ref_sample * 0.1e-3
+    rtf = bio / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rtf, "unit": "x realtime",
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1000.0 * dt / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl["desc"], "steps_per_bench_step": a.ref_sample, "dt_ms": 0.1,
+                   "threads": threads},
+        "cpu_baseline": {"value": rtf, "unit": "x realtime", "cores": threads, "kind": kind,
+                         "sample": f"{a.steps} x {a.ref_sample} exchange steps"},
+        "e2e": {"value": rtf, "unit": "x realtime", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(a):
+    import torch
+
+    import scaffold_gb300 as sg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+    wl = WORKLOADS[a.workload]
+    nets, seeds = build_nets(wl, rank)
+    sim = sg.Simulation(nets, seeds, weight_type=sg.WEIGHT_BF16 if wl["bf16"] else sg.WEIGHT_FP32,
+                        chunk_steps=a.chunk, device=local)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    info = sim.info()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    bio_per_step = a.chunk * 0.1e-3 * len(nets)
+
+    for _ in range(a.warmup):
+        sim.enqueue(a.chunk)
+    sim.sync()
+    ev0 = sim.info().events
+    l0 = sim.launch_count()
+    clocks = Clocks(local)
+    clocks.start()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    evs = []
+    for i in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)  # > L2: every timed step starts from a cold L2
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.enqueue(a.chunk)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    sim.sync()
+    if pg:
+        pg.barrier()
+    clk = clocks.stop()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    events = sim.info().events - ev0
+    launches = sim.launch_count() - l0
+    t = torch.tensor([ms, float(events)], dtype=torch.float64, device="cuda")
+    if pg:
+        tm = t.clone()
+        pg.all_reduce(tm, op=pg.ReduceOp.MAX)
+        pg.all_reduce(t, op=pg.ReduceOp.SUM)
+        ms_max, events_all = float(tm[0]), float(t[1])
+    else:
+        ms_max, events_all = ms, float(events)
+    value = world * a.steps * bio_per_step / (ms_max / 1000.0)
+
+    # End to end through the C ABI: new input rates from host memory before
+    # each step, per-step spike counts of every population back to the host.
+    rates = [4.0, 100.0] if wl["config"] != 1 else [4.0]
+    n_src = len(nets[0].inputs())
+    rates = rates[:n_src]
+    e2e_steps = max(3, min(a.steps, 20))
+    sim.loop_n_steps(a.chunk, counts=True)
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k in range(len(nets)):
+            sim.set_input_freq(k, rates)
+        counts, _ = sim.loop_n_steps(a.chunk, counts=True)
+    e2e_s = time.perf_counter() - t0
+    if pg:
+        te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        pg.all_reduce(te, op=pg.ReduceOp.MAX)
+        e2e_s = float(te[0])
+    e2e = {"value": world * e2e_steps * bio_per_step / e2e_s, "unit": "x realtime",
+           "h2d_bytes_per_step": 56 * n_src * len(nets),
+           "d2h_bytes_per_step": 4 * a.chunk * info.n_segments + 4}
+
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return
+    # Roofline of the dominant kernel from an instrumented run (CUDA events on
+    # the handle's stream around every launch).
+    mean_us, bytes_pl, nl = sim.profile(1000)
+    names = ["k_update", "k_push_csr", "k_pull_thread", "k_pull_warp", "k_advance"]
+    share = [m * n for m, n in zip(mean_us, nl)]
+    dom = max(range(len(names)), key=lambda k: share[k])
+    peak, peak_kind = measured_hbm()
+    achieved = bytes_pl[dom] / (mean_us[dom] * 1e-6) / 1e9 if mean_us[dom] > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get(a.workload, {}).get(names[dom])
+        except ValueError:
+            traffic = None
+    roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+            "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "algorithmic_bytes_per_launch": bytes_pl[dom],
+            "mean_us_per_launch": mean_us[dom],
+            "kernel_time_share": {n: s / max(sum(share), 1e-12) for n, s in zip(names, share)}}
+    cpu = None
+    if not a.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(wl, a.cpu_sample)
+        except Exception as ex:  # report, do not fail the GPU number
+            cpu = {"value": None, "error": str(ex)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "x realtime", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded fixed in-degree connectivity, Philox Poisson mossy input",
+        "config": {"workload": wl["desc"], "cells": info.n_neurons, "synapses": info.n_synapses,
+                   "instances_per_gpu": len(nets), "dt_ms": 0.1,
+                   "steps_per_bench_step": a.chunk, "bio_s_per_bench_step": bio_per_step,
+                   "weights": "bf16" if wl["bf16"] else "fp32", "exec": "cuda graph per chunk",
+                   "propagation": "event-driven CSR push",
+                   "l2": "flushed (256 MiB write) between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "synaptic_events_per_s": events_all / (ms_max / 1000.0),
+        "gpu_launches": launches,
+        "e2e": e2e,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

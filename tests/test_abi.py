@@ -1,0 +1,46 @@
+"""The C-ABI library loads without a GPU and exports every declared symbol."""
+import ctypes as C
+import os
+import re
+
+import scaffold_gb300 as sg
+from scaffold_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "scaffold_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_symbols_exported():
+    names = declared_functions()
+    assert len(names) >= 35
+    lib = C.CDLL(L.LIB_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    assert set(declared_functions()) == set(L.PROTOTYPES)
+
+
+def test_config_defaults_and_errors():
+    cfg = L.Config()
+    L.lib().sgb_config_init(C.byref(cfg))
+    assert (cfg.dt_ms, cfg.substeps, cfg.chunk_steps, cfg.weight_type, cfg.exec_mode) == (
+        0.1, 1, 1000, sg.WEIGHT_FP32, sg.EXEC_GRAPH)
+    assert L.lib().sgb_abi_version() == 1
+    rc = L.lib().sgb_net_create(None)
+    assert rc == -1 and b"NULL" in L.lib().sgb_last_error()
+    assert L.lib().sgb_sim_run(None, 10, None, None, 0, None) == -1
+
+
+def test_struct_sizes_match_header_layout():
+    # The ctypes mirrors must have the C layout of the header's structs.
+    assert C.sizeof(L.Config) == 8 + 4 * 16
+    assert C.sizeof(L.InputParams) == 40
+    assert C.sizeof(L.SegmentInfo) == 32
