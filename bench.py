@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1000,
                     help="exchange steps of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--exec", default="persistent", choices=["persistent", "graph"])
+    ap.add_argument("--blocks-per-sm", type=int, default=1)
     return ap.parse_args()
 
 
@@ -207,8 +209,10 @@ def run_gb300(a):
         pg = dist
     wl = WORKLOADS[a.workload]
     nets, seeds = build_nets(wl, rank)
+    exec_mode = sg.EXEC_PERSISTENT if a.exec == "persistent" else sg.EXEC_GRAPH
     sim = sg.Simulation(nets, seeds, weight_type=sg.WEIGHT_BF16 if wl["bf16"] else sg.WEIGHT_FP32,
-                        chunk_steps=a.chunk, device=local)
+                        chunk_steps=a.chunk, device=local, exec_mode=exec_mode,
+                        blocks_per_sm=a.blocks_per_sm)
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
     info = sim.info()
@@ -283,7 +287,7 @@ def run_gb300(a):
     # Roofline of the dominant kernel from an instrumented run (CUDA events on
     # the handle's stream around every launch).
     mean_us, bytes_pl, nl = sim.profile(1000)
-    names = ["k_update", "k_push_csr", "k_pull_thread", "k_pull_warp", "k_advance"]
+    names = ["k_update", "k_deliver"]
     share = [m * n for m, n in zip(mean_us, nl)]
     dom = max(range(len(names)), key=lambda k: share[k])
     peak, peak_kind = measured_hbm()
@@ -314,7 +318,9 @@ def run_gb300(a):
         "config": {"workload": wl["desc"], "cells": info.n_neurons, "synapses": info.n_synapses,
                    "instances_per_gpu": len(nets), "dt_ms": 0.1,
                    "steps_per_bench_step": a.chunk, "bio_s_per_bench_step": bio_per_step,
-                   "weights": "bf16" if wl["bf16"] else "fp32", "exec": "cuda graph per chunk",
+                   "weights": "bf16" if wl["bf16"] else "fp32",
+                   "exec": ("one persistent cooperative kernel per chunk" if a.exec == "persistent"
+                            else "cuda graph of 2 kernels per step"),
                    "propagation": "event-driven CSR push",
                    "l2": "flushed (256 MiB write) between timed steps",
                    "parallelism": f"replicas x{world}"},

@@ -33,6 +33,7 @@ void sgb_config_init(sgb_config* cfg) {
   cfg->device = 0;
   cfg->default_prop = SGB_PROP_AUTO;
   cfg->raster = 0;
+  cfg->blocks_per_sm = 0;
 }
 
 const char* sgb_last_error(void) { return last_error(); }
@@ -289,7 +290,7 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
     return set_error(SGB_ERR_CUDA, "reading the step counter failed");
   info->step = (int64_t)ctl.step;
   info->events = (int64_t)ctl.events;
-  info->device_bytes = (int64_t)(s.pool_bytes + s.misc_bytes);
+  info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;
   info->weight_type = s.cfg.weight_type;
   info->substeps = s.cfg.substeps;

@@ -13,20 +13,27 @@
 //   history    spike bitmaps of the last H = max delay steps (1 bit per cell).
 //   active     compacted ids of the cells that fired in the current step
 //              (double-buffered by step parity).
-//   tables     per projection: pre-major CSR (event-driven push) and
-//              post-major ELL (dense pull), 32-bit synapse words
-//              (population-local index | delay << 28) plus FP32 or BF16
-//              weights.
+//   push table one cell-major CSR over every projection in event-driven mode
+//              (all instances): synapse word = padded post index | delay << 27
+//              | accumulator << 31, plus the weight pre-multiplied by its
+//              accumulator's 2^S (exact power-of-two scaling) in FP32 or BF16.
+//   ELL tables per projection, post-major (dense pull): word = population-local
+//              pre index | delay << 28, plus the pre-scaled weight.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace sgb {
 
-constexpr int kUpdateTile = 256;      // cells per update block (8 warps)
-constexpr int kPullThreadTile = 128;  // posts per block of the column-major ELL pull
+constexpr int kBlock = 256;           // threads per block of every step kernel
 constexpr int kPullWarpChunk = 1024;  // synapses per warp item of the row-major ELL pull
 constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-major layout
+// Push-table synapse word: 27-bit padded post index, 4-bit delay, 1-bit accumulator.
+constexpr uint32_t kPushPostBits = 27;
+constexpr uint32_t kPushPostMask = (1u << kPushPostBits) - 1u;
+// Grid-barrier spin limit (iterations of ~64 ns sleeps): ~1 s, then the
+// kernel records kErrBarrierTimeout and returns.
+constexpr uint32_t kBarrierSpinLimit = 1u << 24;
 
 enum SegKind : uint32_t { kSegLif = 0, kSegInput = 1 };
 
@@ -58,11 +65,8 @@ struct ProjDev {
   uint32_t ell_K;                 // ELL width (max in-degree)
   uint32_t ell_rowmajor;          // 0: [K][post_count], 1: [post_count][K]
   uint32_t pad_;
-  const uint32_t* csr_row;        // [pre_count + 1]
-  const uint32_t* csr_syn;        // post | delay << 28
-  const void* csr_w;
   const uint32_t* ell_syn;        // pre | delay << 28, kEllPad for padding
-  const void* ell_w;
+  const void* ell_w;              // weights x 2^S
 };
 
 struct SrcDev {
@@ -91,9 +95,8 @@ struct Ctl {
 constexpr uint32_t kErrRasterOverflow = 1u;
 constexpr uint32_t kErrBarrierTimeout = 2u;
 
-struct PullTile { uint32_t proj, post_start; };
-struct PullItem { uint32_t proj, post, k0; };
-struct UpdTile { uint32_t seg, start; };
+struct PullTile { uint32_t proj, post_start; };   // 32 posts of a column-major ELL
+struct PullItem { uint32_t proj, post, k0; };      // one row chunk of a row-major ELL
 
 // Everything a step kernel needs, passed by value.
 struct StepArgs {
@@ -105,7 +108,10 @@ struct StepArgs {
   const uint16_t* seg_of_word;    // segment of each 32-cell word
   const uint32_t* src_mask;       // per cell: bit s = covered by source s of its segment
   const uint32_t* outdeg;         // per cell: synapses leaving it (all projections)
-  const UpdTile* upd_tiles;
+  const uint32_t* upd_words;      // 32-cell words holding cells (padding words skipped)
+  const uint32_t* push_row;       // [n_pad + 1] push-table row offsets
+  const uint32_t* push_syn;
+  const void* push_w;
   const PullTile* pull_tiles;
   const PullItem* pull_items;
   float4* state;
@@ -116,9 +122,11 @@ struct StepArgs {
   uint32_t* raster;               // [raster_cap] padded ids
   uint32_t* raster_off;           // [chunk_steps + 1]
   double* totals;                 // [n_segs]
+  unsigned long long* bar;        // grid-barrier arrival counter (zeroed per launch)
   uint32_t n_pad, n_words, n_segs, n_projs;
   uint32_t ring_slots, hist_rows;
-  uint32_t n_upd_tiles, n_pull_tiles, n_pull_items;
+  uint32_t n_upd_words, n_pull_tiles, n_pull_items;
+  uint32_t any_push;
   uint32_t raster_cap;
   int32_t bf16;
   int32_t substeps;
@@ -127,10 +135,11 @@ struct StepArgs {
 // Launch wrappers (sgb_kernels.cu).  All return the launch status.
 cudaError_t launch_chunk_begin(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_update(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_push(const StepArgs& a, int blocks, cudaStream_t s);
-cudaError_t launch_pull_thread(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_pull_warp(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_advance(const StepArgs& a, cudaStream_t s);
+// Delivery of the current step; also advances the step counter.
+cudaError_t launch_deliver(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s);
+// One cooperative launch advancing n_steps; grid = blocks (all co-resident).
+cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s);
+int persistent_blocks_per_sm(bool bf16);
 
 }  // namespace sgb

@@ -4,9 +4,10 @@
 // The reference's equivalents are Initialization (GPUScaffoldSimulation.cu:
 // 132-631: population split, ELL upload, Philox state setup, streams) and
 // loop_n_steps (:693-791: per-ms launches on 12 streams + a device-wide
-// synchronize).  Here one handle holds any number of independent instances;
-// a chunk of steps is captured once as a CUDA graph whose step index lives in
-// device memory, so the same executable graph is replayed for every chunk.
+// synchronize).  Here one handle holds any number of independent instances.
+// Two drivers advance a chunk of steps: a CUDA graph of two kernels per step
+// whose step index lives in device memory (so one executable graph is
+// replayed for every chunk), or one persistent cooperative kernel per chunk.
 #include "sgb_engine.h"
 
 #include <math.h>
@@ -33,12 +34,15 @@ namespace sgb {
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 Sim::~Sim() {
+  if (stream) cudaStreamSynchronize(stream);
   for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
-  if (d_pool) cudaFree(d_pool);
+  if (d_ell) cudaFree(d_ell);
+  if (d_push) cudaFree(d_push);
   if (d_misc) cudaFree(d_misc);
   if (h_counts) cudaFreeHost(h_counts);
   if (h_raster) cudaFreeHost(h_raster);
   if (h_raster_off) cudaFreeHost(h_raster_off);
+  if (h_srcs) cudaFreeHost(h_srcs);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
 
@@ -98,39 +102,21 @@ static float initial_u(const Population& p, uint64_t seed, uint32_t key) {
   return fmaf(p.Vth - p.Vr, u01_open0(r.x), p.Vr);
 }
 
+// Weight as stored in a device table: the (BF16-rounded) magnitude times the
+// accumulator's 2^S.  Power-of-two scaling is exact, so rint(stored) equals
+// rint(w * 2^S) for the table's w.
+static float scaled_weight(float w, int32_t bits, bool bf16) {
+  return ldexpf(table_weight(w, bf16), bits);
+}
+
 // ---------------------------------------------------------------------------
-namespace {
-
-struct HostTables {
-  std::vector<uint32_t> csr_row, csr_syn, ell_syn;
-  std::vector<float> csr_wf, ell_wf;
-  std::vector<uint16_t> csr_wh, ell_wh;
-};
-
-void build_tables(const Projection& pr, int32_t npre, int32_t npost, bool bf16, ProjTables& t,
-                  HostTables& h) {
+// Post-major ELL of one projection, width = max in-degree, padding at the end
+// of each row; column-major for narrow rows (one thread per post), row-major
+// for wide ones (one warp per row chunk).
+static void build_ell(const Projection& pr, int32_t npost, bool bf16, ProjTables& t,
+                      std::vector<uint32_t>& syn, std::vector<float>& wf,
+                      std::vector<uint16_t>& wh) {
   const size_t nnz = pr.pre_idx.size();
-  t.nnz = (int64_t)nnz;
-  // Pre-major CSR, synapses of a row in stored order.
-  h.csr_row.assign((size_t)npre + 1, 0);
-  for (size_t i = 0; i < nnz; ++i) h.csr_row[pr.pre_idx[i] + 1]++;
-  int32_t mx = 0;
-  for (int32_t j = 0; j < npre; ++j) {
-    mx = std::max<int32_t>(mx, (int32_t)h.csr_row[j + 1]);
-    h.csr_row[j + 1] += h.csr_row[j];
-  }
-  t.max_out = mx;
-  h.csr_syn.resize(nnz);
-  if (bf16) h.csr_wh.resize(nnz); else h.csr_wf.resize(nnz);
-  {
-    std::vector<uint32_t> fill(h.csr_row.begin(), h.csr_row.end() - 1);
-    for (size_t i = 0; i < nnz; ++i) {
-      const uint32_t q = fill[pr.pre_idx[i]]++;
-      h.csr_syn[q] = syn_pack(pr.post_idx[i], pr.delay[i]);
-      if (bf16) h.csr_wh[q] = f32_to_bf16_bits(pr.weight[i]); else h.csr_wf[q] = pr.weight[i];
-    }
-  }
-  // Post-major ELL, width = max in-degree, padding at the end of each row.
   std::vector<uint32_t> indeg((size_t)npost, 0);
   for (size_t i = 0; i < nnz; ++i) indeg[pr.post_idx[i]]++;
   uint32_t K = 0;
@@ -138,41 +124,88 @@ void build_tables(const Projection& pr, int32_t npre, int32_t npost, bool bf16, 
   t.ell_K = K;
   t.ell_rowmajor = K > kEllColMajorMaxK;
   const size_t cells = (size_t)K * (size_t)npost;
-  h.ell_syn.assign(cells, kEllPad);
-  if (bf16) h.ell_wh.assign(cells, 0); else h.ell_wf.assign(cells, 0.f);
+  syn.assign(cells, kEllPad);
+  if (bf16) wh.assign(cells, 0); else wf.assign(cells, 0.f);
   std::vector<uint32_t> col((size_t)npost, 0);
   for (size_t i = 0; i < nnz; ++i) {
     const uint32_t p = pr.post_idx[i];
     const uint32_t k = col[p]++;
     const size_t q = t.ell_rowmajor ? (size_t)p * K + k : (size_t)k * npost + p;
-    h.ell_syn[q] = syn_pack(pr.pre_idx[i], pr.delay[i]);
-    if (bf16) h.ell_wh[q] = f32_to_bf16_bits(pr.weight[i]); else h.ell_wf[q] = pr.weight[i];
+    syn[q] = syn_pack(pr.pre_idx[i], pr.delay[i]);
+    const float w = scaled_weight(pr.weight[i], t.scale_bits, bf16);
+    if (bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
   }
 }
 
-}  // namespace
-
-// ---------------------------------------------------------------------------
-static int rebuild_work_lists(Sim& s, std::vector<PullTile>& tiles, std::vector<PullItem>& items) {
-  tiles.clear();
-  items.clear();
+// Rebuilds the merged push table (every projection in CSR mode, cell-major)
+// and the dense-pull work lists, uploads them, and drops captured graphs.
+static int upload_modes(Sim& s) {
+  StepArgs& a = s.args;
+  // Push table.
+  std::vector<uint32_t> row((size_t)s.n_pad + 1, 0);
+  int64_t total = 0;
+  for (size_t k = 0; k < s.projs.size(); ++k) {
+    if (s.projs[k].mode != SGB_PROP_CSR) continue;
+    const ProjTables& t = s.ptab[k];
+    const Projection& pr = s.nets[t.net].projs[t.proj];
+    const uint32_t pre_base = s.segs[t.pre_seg].base;
+    for (uint32_t p : pr.pre_idx) row[pre_base + p + 1]++;
+    total += t.nnz;
+  }
+  if (total > 0xFFFFFFFFll) return set_error(SGB_ERR_UNSUPPORTED, "more than 2^32 push synapses");
+  for (uint32_t j = 0; j < s.n_pad; ++j) row[j + 1] += row[j];
+  std::vector<uint32_t> syn((size_t)total);
+  std::vector<float> wf(s.bf16 ? 0 : (size_t)total);
+  std::vector<uint16_t> wh(s.bf16 ? (size_t)total : 0);
+  {
+    std::vector<uint32_t> fill(row.begin(), row.end() - 1);
+    for (size_t k = 0; k < s.projs.size(); ++k) {
+      if (s.projs[k].mode != SGB_PROP_CSR) continue;
+      const ProjTables& t = s.ptab[k];
+      const Projection& pr = s.nets[t.net].projs[t.proj];
+      const uint32_t pre_base = s.segs[t.pre_seg].base, post_base = s.segs[t.post_seg].base;
+      for (size_t i = 0; i < pr.pre_idx.size(); ++i) {
+        const uint32_t q = fill[pre_base + pr.pre_idx[i]]++;
+        syn[q] = (post_base + pr.post_idx[i]) | ((uint32_t)pr.delay[i] << kPushPostBits) |
+                 ((uint32_t)pr.channel << 31);
+        const float w = scaled_weight(pr.weight[i], t.scale_bits, s.bf16);
+        if (s.bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
+      }
+    }
+  }
+  const size_t wsz = s.bf16 ? 2 : 4;
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  SGB_CUDA(cudaMemcpy((void*)a.push_row, row.data(), row.size() * 4, cudaMemcpyHostToDevice));
+  if (total) {
+    SGB_CUDA(cudaMemcpy((void*)a.push_syn, syn.data(), (size_t)total * 4, cudaMemcpyHostToDevice));
+    SGB_CUDA(cudaMemcpy((void*)a.push_w, s.bf16 ? (const void*)wh.data() : (const void*)wf.data(),
+                        (size_t)total * wsz, cudaMemcpyHostToDevice));
+  }
+  a.any_push = total > 0 ? 1u : 0u;
+  // Dense-pull work lists.
+  std::vector<PullTile> tiles;
+  std::vector<PullItem> items;
   for (uint32_t pid = 0; pid < s.projs.size(); ++pid) {
     const ProjDev& P = s.projs[pid];
     if (P.mode != SGB_PROP_ELL || P.ell_K == 0) continue;
     if (!P.ell_rowmajor) {
-      for (uint32_t p0 = 0; p0 < P.post_count; p0 += kPullThreadTile) tiles.push_back({pid, p0});
+      for (uint32_t p0 = 0; p0 < P.post_count; p0 += 32) tiles.push_back({pid, p0});
     } else {
       for (uint32_t p = 0; p < P.post_count; ++p)
         for (uint32_t k0 = 0; k0 < P.ell_K; k0 += kPullWarpChunk) items.push_back({pid, p, k0});
     }
   }
+  if (!tiles.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.pull_tiles, tiles.data(), tiles.size() * sizeof(PullTile), cudaMemcpyHostToDevice));
+  if (!items.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.pull_items, items.data(), items.size() * sizeof(PullItem), cudaMemcpyHostToDevice));
+  SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
+  a.n_pull_tiles = (uint32_t)tiles.size();
+  a.n_pull_items = (uint32_t)items.size();
+  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
+  s.graphs.clear();
   return SGB_OK;
 }
-
-struct MiscLayout {
-  size_t ctl, segs, projs, srcs, out_list, seg_of_word, src_mask, outdeg, upd_tiles, pull_tiles,
-      pull_items, state, ring, hist, active, counts, raster, raster_off, totals, total;
-};
 
 int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seeds, int32_t n,
                Sim** out) {
@@ -188,11 +221,11 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     return set_error(SGB_ERR_ARG, "unknown weight type %d", cfg.weight_type);
   if (cfg.exec_mode < SGB_EXEC_GRAPH || cfg.exec_mode > SGB_EXEC_STREAM)
     return set_error(SGB_ERR_ARG, "unknown exec mode %d", cfg.exec_mode);
-  if (cfg.exec_mode == SGB_EXEC_PERSISTENT)
-    return set_error(SGB_ERR_UNSUPPORTED, "persistent execution is not available in this build");
   if (cfg.default_prop != SGB_PROP_AUTO && cfg.default_prop != SGB_PROP_CSR &&
       cfg.default_prop != SGB_PROP_ELL)
     return set_error(SGB_ERR_ARG, "unknown default propagation mode %d", cfg.default_prop);
+  if (cfg.blocks_per_sm < 0 || cfg.blocks_per_sm > 32)
+    return set_error(SGB_ERR_ARG, "blocks_per_sm %d not in 0..32", cfg.blocks_per_sm);
   for (int32_t i = 0; i < n; ++i)
     if (!nets[i]) return set_error(SGB_ERR_ARG, "network %d is NULL", i);
 
@@ -206,12 +239,11 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     s.nets.push_back(nets[i]->net);
     s.seeds.push_back(seeds ? seeds[i] : (uint64_t)(i + 1));
   }
-  int dev = cfg.device;
-  SGB_CUDA(cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, dev));
+  SGB_CUDA(cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, cfg.device));
   SGB_CUDA(cudaStreamCreateWithFlags(&s.own_stream, cudaStreamNonBlocking));
   s.stream = s.own_stream;
 
-  // ---- segments -----------------------------------------------------------
+  // ---- segments (cells of every instance, each population 32-aligned) -----
   uint64_t cursor = 0;
   int64_t first_id = 0;
   int max_delay = 1;
@@ -242,7 +274,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       cursor += (uint64_t)p.num;
       key += (uint32_t)p.num;
       first_id += p.num;
-      if (cursor > 0xFFFFFF00ull) return set_error(SGB_ERR_UNSUPPORTED, "more than 2^32 cells");
+      if (cursor > kPushPostMask)
+        return set_error(SGB_ERR_UNSUPPORTED, "more than 2^27 cells (with padding) in one handle");
     }
     for (const auto& pr : net.projs)
       for (uint8_t d : pr.delay) max_delay = std::max(max_delay, (int)d);
@@ -254,13 +287,12 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   s.ring_slots = (uint32_t)max_delay + 1;
   s.hist_rows = (uint32_t)max_delay;
 
-  // ---- sources ------------------------------------------------------------
+  // ---- stimulus sources ----------------------------------------------------
   std::vector<uint32_t> src_mask(s.n_pad, 0);
   for (int32_t ni = 0; ni < n; ++ni) {
     const Network& net = s.nets[ni];
-    s.net_src0.push_back((int32_t)s.srcs.size());
-    // Sources grouped by population so that each segment's are contiguous;
-    // within a net, sources keep their definition order.
+    // Each segment's sources are contiguous; bit b of a cell's mask is the
+    // segment's b-th source.
     for (size_t pi = 0; pi < net.pops.size(); ++pi) {
       SegDev& d = s.segs[s.net_seg0[ni] + pi];
       d.src_first = (uint32_t)s.srcs.size();
@@ -279,10 +311,11 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     }
   }
 
-  // ---- projections and tables --------------------------------------------
-  std::vector<HostTables> host(0);
-  std::vector<std::vector<uint32_t>> seg_out(s.segs.size());
+  // ---- projections: ELL tables, out-degrees ---------------------------------
   std::vector<uint32_t> outdeg(s.n_pad, 0);
+  std::vector<std::vector<uint32_t>> ell_syn;
+  std::vector<std::vector<float>> ell_wf;
+  std::vector<std::vector<uint16_t>> ell_wh;
   size_t pool = 0;
   const size_t wsz = s.bf16 ? 2 : 4;
   for (int32_t ni = 0; ni < n; ++ni) {
@@ -296,175 +329,163 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       t.proj = (int32_t)pj;
       t.pre_seg = (uint32_t)(s.net_seg0[ni] + pr.pre);
       t.post_seg = (uint32_t)(s.net_seg0[ni] + pr.post);
-      host.emplace_back();
-      build_tables(pr, net.pops[pr.pre].num, net.pops[pr.post].num, s.bf16, t, host.back());
-      const HostTables& h = host.back();
-      t.off_csr_row = pool; pool = align_up(pool + h.csr_row.size() * 4, 256);
-      t.off_csr_syn = pool; pool = align_up(pool + h.csr_syn.size() * 4, 256);
-      t.off_csr_w = pool; pool = align_up(pool + (size_t)t.nnz * wsz, 256);
-      t.off_ell_syn = pool; pool = align_up(pool + h.ell_syn.size() * 4, 256);
-      t.off_ell_w = pool; pool = align_up(pool + h.ell_syn.size() * wsz, 256);
-      ProjDev P;
-      memset(&P, 0, sizeof P);
+      t.scale_bits = bits[pr.post * 2 + pr.channel];
+      t.nnz = (int64_t)pr.pre_idx.size();
+      ell_syn.emplace_back();
+      ell_wf.emplace_back();
+      ell_wh.emplace_back();
+      build_ell(pr, net.pops[pr.post].num, s.bf16, t, ell_syn.back(), ell_wf.back(), ell_wh.back());
+      t.off_ell_syn = pool;
+      pool = align_up(pool + ell_syn.back().size() * 4, 256);
+      t.off_ell_w = pool;
+      pool = align_up(pool + ell_syn.back().size() * wsz, 256);
       const SegDev& pre = s.segs[t.pre_seg];
       const SegDev& post = s.segs[t.post_seg];
+      for (uint32_t p : pr.pre_idx) outdeg[pre.base + p]++;
+      ProjDev P;
+      memset(&P, 0, sizeof P);
       P.pre_base = pre.base;
       P.post_base = post.base;
       P.pre_count = pre.count;
       P.post_count = post.count;
       P.channel = (uint32_t)pr.channel;
-      int mode = pr.mode == SGB_PROP_AUTO ? cfg.default_prop : pr.mode;
+      const int mode = pr.mode == SGB_PROP_AUTO ? cfg.default_prop : pr.mode;
       P.mode = (uint32_t)(mode == SGB_PROP_AUTO ? SGB_PROP_CSR : mode);
-      P.scale = ldexpf(1.0f, bits[pr.post * 2 + pr.channel]);
+      P.scale = ldexpf(1.0f, t.scale_bits);
       P.ell_K = t.ell_K;
       P.ell_rowmajor = t.ell_rowmajor ? 1u : 0u;
-      seg_out[t.pre_seg].push_back((uint32_t)s.projs.size());
-      for (int32_t j = 0; j < pre.count; ++j)
-        outdeg[pre.base + j] += h.csr_row[j + 1] - h.csr_row[j];
       s.n_syn += t.nnz;
       s.projs.push_back(P);
       s.ptab.push_back(t);
     }
   }
-  std::vector<uint32_t> out_list;
-  for (size_t si = 0; si < s.segs.size(); ++si) {
-    s.segs[si].out_first = (uint32_t)out_list.size();
-    s.segs[si].out_count = (uint32_t)seg_out[si].size();
-    out_list.insert(out_list.end(), seg_out[si].begin(), seg_out[si].end());
-  }
-  std::vector<uint16_t> seg_of_word(s.n_words, 0);
-  std::vector<UpdTile> upd;
+  std::vector<uint16_t> seg_of_word(s.n_words, 0xFFFF);
+  std::vector<uint32_t> upd_words;
   for (size_t si = 0; si < s.segs.size(); ++si) {
     const SegDev& d = s.segs[si];
-    for (uint32_t w = d.base / 32; w < (d.base + d.count + 31) / 32; ++w) seg_of_word[w] = (uint16_t)si;
-    for (uint32_t st = d.base; st < d.base + d.count; st += kUpdateTile) upd.push_back({(uint32_t)si, st});
+    for (uint32_t w = d.base / 32; w < (d.base + d.count + 31) / 32; ++w) {
+      seg_of_word[w] = (uint16_t)si;
+      upd_words.push_back(w);
+    }
   }
-  std::vector<PullTile> ptiles;
-  std::vector<PullItem> pitems;
-  rebuild_work_lists(s, ptiles, pitems);
-  // Capacity for every projection in ELL mode, so modes can change later.
   size_t cap_tiles = 0, cap_items = 0;
   for (const ProjDev& P : s.projs) {
     if (!P.ell_K) continue;
-    if (!P.ell_rowmajor) cap_tiles += (P.post_count + kPullThreadTile - 1) / kPullThreadTile;
+    if (!P.ell_rowmajor) cap_tiles += (P.post_count + 31) / 32;
     else cap_items += (size_t)P.post_count * ((P.ell_K + kPullWarpChunk - 1) / kPullWarpChunk);
   }
 
-  // ---- device memory -------------------------------------------------------
-  s.pool_bytes = std::max<size_t>(pool, 256);
-  SGB_CUDA(cudaMalloc(&s.d_pool, s.pool_bytes));
+  // ---- device memory ---------------------------------------------------------
+  s.ell_bytes = std::max<size_t>(pool, 256);
+  SGB_CUDA(cudaMalloc(&s.d_ell, s.ell_bytes));
   for (size_t i = 0; i < s.ptab.size(); ++i) {
     const ProjTables& t = s.ptab[i];
-    const HostTables& h = host[i];
-    char* base = (char*)s.d_pool;
-    SGB_CUDA(cudaMemcpy(base + t.off_csr_row, h.csr_row.data(), h.csr_row.size() * 4, cudaMemcpyHostToDevice));
-    if (t.nnz) {
-      SGB_CUDA(cudaMemcpy(base + t.off_csr_syn, h.csr_syn.data(), h.csr_syn.size() * 4, cudaMemcpyHostToDevice));
-      SGB_CUDA(cudaMemcpy(base + t.off_csr_w, s.bf16 ? (const void*)h.csr_wh.data() : (const void*)h.csr_wf.data(),
-                          (size_t)t.nnz * wsz, cudaMemcpyHostToDevice));
+    char* base = (char*)s.d_ell;
+    if (!ell_syn[i].empty()) {
+      SGB_CUDA(cudaMemcpy(base + t.off_ell_syn, ell_syn[i].data(), ell_syn[i].size() * 4, cudaMemcpyHostToDevice));
+      SGB_CUDA(cudaMemcpy(base + t.off_ell_w, s.bf16 ? (const void*)ell_wh[i].data() : (const void*)ell_wf[i].data(),
+                          ell_syn[i].size() * wsz, cudaMemcpyHostToDevice));
     }
-    if (!h.ell_syn.empty()) {
-      SGB_CUDA(cudaMemcpy(base + t.off_ell_syn, h.ell_syn.data(), h.ell_syn.size() * 4, cudaMemcpyHostToDevice));
-      SGB_CUDA(cudaMemcpy(base + t.off_ell_w, s.bf16 ? (const void*)h.ell_wh.data() : (const void*)h.ell_wf.data(),
-                          h.ell_syn.size() * wsz, cudaMemcpyHostToDevice));
-    }
-    ProjDev& P = s.projs[i];
-    P.csr_row = (const uint32_t*)(base + t.off_csr_row);
-    P.csr_syn = (const uint32_t*)(base + t.off_csr_syn);
-    P.csr_w = base + t.off_csr_w;
-    P.ell_syn = (const uint32_t*)(base + t.off_ell_syn);
-    P.ell_w = base + t.off_ell_w;
+    s.projs[i].ell_syn = (const uint32_t*)(base + t.off_ell_syn);
+    s.projs[i].ell_w = base + t.off_ell_w;
+    std::vector<uint32_t>().swap(ell_syn[i]);
+    std::vector<float>().swap(ell_wf[i]);
+    std::vector<uint16_t>().swap(ell_wh[i]);
   }
-  host.clear();
-  host.shrink_to_fit();
+  {
+    size_t p = 0;
+    const size_t off_row = p; p = align_up(p + ((size_t)s.n_pad + 1) * 4, 256);
+    const size_t off_syn = p; p = align_up(p + std::max<int64_t>(s.n_syn, 1) * 4, 256);
+    const size_t off_w = p; p = align_up(p + std::max<int64_t>(s.n_syn, 1) * wsz, 256);
+    s.push_bytes = p;
+    SGB_CUDA(cudaMalloc(&s.d_push, s.push_bytes));
+    s.args.push_row = (const uint32_t*)((char*)s.d_push + off_row);
+    s.args.push_syn = (const uint32_t*)((char*)s.d_push + off_syn);
+    s.args.push_w = (const void*)((char*)s.d_push + off_w);
+  }
 
   s.raster_cap = cfg.raster ? (uint32_t)std::min<uint64_t>((uint64_t)s.n_pad * s.chunk, 1ull << 24) : 0;
   const size_t nseg = s.segs.size();
-  MiscLayout L;
   size_t m = 0;
   auto take = [&](size_t bytes) { size_t o = m; m = align_up(m + std::max<size_t>(bytes, 1), 256); return o; };
-  L.ctl = take(sizeof(Ctl));
-  L.segs = take(nseg * sizeof(SegDev));
-  L.projs = take(std::max<size_t>(s.projs.size(), 1) * sizeof(ProjDev));
-  L.srcs = take(std::max<size_t>(s.srcs.size(), 1) * sizeof(SrcDev));
-  L.out_list = take(std::max<size_t>(out_list.size(), 1) * 4);
-  L.seg_of_word = take((size_t)s.n_words * 2);
-  L.src_mask = take((size_t)s.n_pad * 4);
-  L.outdeg = take((size_t)s.n_pad * 4);
-  L.upd_tiles = take(std::max<size_t>(upd.size(), 1) * sizeof(UpdTile));
-  L.pull_tiles = take(std::max<size_t>(cap_tiles, 1) * sizeof(PullTile));
-  L.pull_items = take(std::max<size_t>(cap_items, 1) * sizeof(PullItem));
-  L.state = take((size_t)s.n_pad * sizeof(float4));
-  L.ring = take((size_t)s.ring_slots * s.n_pad * 8);
-  L.hist = take((size_t)s.hist_rows * s.n_words * 4);
-  L.active = take((size_t)2 * s.n_pad * 4);
-  L.counts = take((size_t)s.chunk * nseg * 4);
-  L.raster = take((size_t)std::max<uint32_t>(s.raster_cap, 1) * 4);
-  L.raster_off = take((size_t)(s.chunk + 1) * 4);
-  L.totals = take(nseg * sizeof(double));
-  L.total = m;
+  const size_t o_ctl = take(sizeof(Ctl));
+  const size_t o_bar = take(sizeof(unsigned long long));
+  const size_t o_segs = take(nseg * sizeof(SegDev));
+  const size_t o_projs = take(std::max<size_t>(s.projs.size(), 1) * sizeof(ProjDev));
+  const size_t o_srcs = take(std::max<size_t>(s.srcs.size(), 1) * sizeof(SrcDev));
+  const size_t o_sow = take((size_t)s.n_words * 2);
+  const size_t o_mask = take((size_t)s.n_pad * 4);
+  const size_t o_outdeg = take((size_t)s.n_pad * 4);
+  const size_t o_words = take(std::max<size_t>(upd_words.size(), 1) * 4);
+  const size_t o_tiles = take(std::max<size_t>(cap_tiles, 1) * sizeof(PullTile));
+  const size_t o_items = take(std::max<size_t>(cap_items, 1) * sizeof(PullItem));
+  const size_t o_state = take((size_t)s.n_pad * sizeof(float4));
+  const size_t o_ring = take((size_t)s.ring_slots * s.n_pad * 8);
+  const size_t o_hist = take((size_t)s.hist_rows * s.n_words * 4);
+  const size_t o_active = take((size_t)2 * s.n_pad * 4);
+  const size_t o_counts = take((size_t)s.chunk * nseg * 4);
+  const size_t o_raster = take((size_t)std::max<uint32_t>(s.raster_cap, 1) * 4);
+  const size_t o_roff = take((size_t)(s.chunk + 1) * 4);
+  const size_t o_totals = take(nseg * sizeof(double));
   s.misc_bytes = m;
   SGB_CUDA(cudaMalloc(&s.d_misc, s.misc_bytes));
   SGB_CUDA(cudaMemset(s.d_misc, 0, s.misc_bytes));
   char* mb = (char*)s.d_misc;
 
   StepArgs& a = s.args;
-  memset(&a, 0, sizeof a);
-  a.ctl = (Ctl*)(mb + L.ctl);
-  a.segs = (const SegDev*)(mb + L.segs);
-  a.projs = (const ProjDev*)(mb + L.projs);
-  a.srcs = (const SrcDev*)(mb + L.srcs);
-  a.out_list = (const uint32_t*)(mb + L.out_list);
-  a.seg_of_word = (const uint16_t*)(mb + L.seg_of_word);
-  a.src_mask = (const uint32_t*)(mb + L.src_mask);
-  a.outdeg = (const uint32_t*)(mb + L.outdeg);
-  a.upd_tiles = (const UpdTile*)(mb + L.upd_tiles);
-  a.pull_tiles = (const PullTile*)(mb + L.pull_tiles);
-  a.pull_items = (const PullItem*)(mb + L.pull_items);
-  a.state = (float4*)(mb + L.state);
-  a.ring = (int*)(mb + L.ring);
-  a.hist = (uint32_t*)(mb + L.hist);
-  a.active = (uint32_t*)(mb + L.active);
-  a.counts = (uint32_t*)(mb + L.counts);
-  a.raster = (uint32_t*)(mb + L.raster);
-  a.raster_off = (uint32_t*)(mb + L.raster_off);
-  a.totals = (double*)(mb + L.totals);
+  a.ctl = (Ctl*)(mb + o_ctl);
+  a.bar = (unsigned long long*)(mb + o_bar);
+  a.segs = (const SegDev*)(mb + o_segs);
+  a.projs = (const ProjDev*)(mb + o_projs);
+  a.srcs = (const SrcDev*)(mb + o_srcs);
+  a.seg_of_word = (const uint16_t*)(mb + o_sow);
+  a.src_mask = (const uint32_t*)(mb + o_mask);
+  a.outdeg = (const uint32_t*)(mb + o_outdeg);
+  a.upd_words = (const uint32_t*)(mb + o_words);
+  a.pull_tiles = (const PullTile*)(mb + o_tiles);
+  a.pull_items = (const PullItem*)(mb + o_items);
+  a.state = (float4*)(mb + o_state);
+  a.ring = (int*)(mb + o_ring);
+  a.hist = (uint32_t*)(mb + o_hist);
+  a.active = (uint32_t*)(mb + o_active);
+  a.counts = (uint32_t*)(mb + o_counts);
+  a.raster = (uint32_t*)(mb + o_raster);
+  a.raster_off = (uint32_t*)(mb + o_roff);
+  a.totals = (double*)(mb + o_totals);
   a.n_pad = s.n_pad;
   a.n_words = s.n_words;
   a.n_segs = (uint32_t)nseg;
   a.n_projs = (uint32_t)s.projs.size();
   a.ring_slots = s.ring_slots;
   a.hist_rows = s.hist_rows;
-  a.n_upd_tiles = (uint32_t)upd.size();
-  a.n_pull_tiles = (uint32_t)ptiles.size();
-  a.n_pull_items = (uint32_t)pitems.size();
+  a.n_upd_words = (uint32_t)upd_words.size();
   a.raster_cap = s.raster_cap;
   a.bf16 = s.bf16 ? 1 : 0;
   a.substeps = cfg.substeps;
-  s.push_blocks = 2 * s.sm_count;
+  s.deliver_blocks = 2 * s.sm_count;
+  const int bpsm = std::min(cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : 1,
+                            persistent_blocks_per_sm(s.bf16));
+  s.persistent_blocks = std::max(1, bpsm) * s.sm_count;
 
   SGB_CUDA(cudaMemcpy((void*)a.segs, s.segs.data(), nseg * sizeof(SegDev), cudaMemcpyHostToDevice));
-  if (!s.projs.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
-  if (!s.srcs.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.srcs, s.srcs.data(), s.srcs.size() * sizeof(SrcDev), cudaMemcpyHostToDevice));
-  if (!out_list.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.out_list, out_list.data(), out_list.size() * 4, cudaMemcpyHostToDevice));
+  SGB_CUDA(cudaMallocHost(&s.h_srcs, std::max<size_t>(s.srcs.size(), 1) * sizeof(SrcDev)));
+  if (!s.srcs.empty()) {
+    memcpy(s.h_srcs, s.srcs.data(), s.srcs.size() * sizeof(SrcDev));
+    SGB_CUDA(cudaMemcpy((void*)a.srcs, s.h_srcs, s.srcs.size() * sizeof(SrcDev), cudaMemcpyHostToDevice));
+  }
   SGB_CUDA(cudaMemcpy((void*)a.seg_of_word, seg_of_word.data(), seg_of_word.size() * 2, cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMemcpy((void*)a.src_mask, src_mask.data(), src_mask.size() * 4, cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMemcpy((void*)a.outdeg, outdeg.data(), outdeg.size() * 4, cudaMemcpyHostToDevice));
-  if (!upd.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.upd_tiles, upd.data(), upd.size() * sizeof(UpdTile), cudaMemcpyHostToDevice));
-  if (!ptiles.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.pull_tiles, ptiles.data(), ptiles.size() * sizeof(PullTile), cudaMemcpyHostToDevice));
-  if (!pitems.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.pull_items, pitems.data(), pitems.size() * sizeof(PullItem), cudaMemcpyHostToDevice));
+  if (!upd_words.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.upd_words, upd_words.data(), upd_words.size() * 4, cudaMemcpyHostToDevice));
+  int rc = upload_modes(s);
+  if (rc) return rc;
 
   SGB_CUDA(cudaMallocHost(&s.h_counts, (size_t)s.chunk * nseg * 4));
   SGB_CUDA(cudaMallocHost(&s.h_raster_off, (size_t)(s.chunk + 1) * 4));
   if (s.raster_cap) SGB_CUDA(cudaMallocHost(&s.h_raster, (size_t)s.raster_cap * 4));
 
-  int rc = sim_reset(s, nullptr);
+  rc = sim_reset(s, nullptr);
   if (rc) return rc;
   *out = S.release();
   return SGB_OK;
@@ -483,8 +504,7 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
     const SegDev& d = s.segs[si];
     if (d.kind != kSegLif) continue;
     const Population& p = s.nets[s.seg_net[si]].pops[s.seg_pop[si]];
-    for (uint32_t j = 0; j < d.count; ++j)
-      st[d.base + j].x = initial_u(p, d.seed, d.key_base + j);
+    for (uint32_t j = 0; j < d.count; ++j) st[d.base + j].x = initial_u(p, d.seed, d.key_base + j);
   }
   const StepArgs& a = s.args;
   SGB_CUDA(cudaMemcpyAsync(a.state, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, s.stream));
@@ -498,7 +518,7 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
 
 // ---------------------------------------------------------------------------
 // One chunk of c steps issued on `st` (direct launches; also the body that is
-// captured into a graph).
+// captured into a graph).  *nlaunch receives the number of kernel launches.
 static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nlaunch) {
   const StepArgs& a = s.args;
   cudaError_t e;
@@ -506,21 +526,16 @@ static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nla
   if ((e = cudaMemsetAsync(a.counts, 0, (size_t)c * a.n_segs * 4, st))) return e;
   if ((e = launch_chunk_begin(a, st))) return e;
   L++;
-  bool any_csr = false;
-  for (const ProjDev& P : s.projs) any_csr |= P.mode == SGB_PROP_CSR && P.pre_count && P.post_count;
-  for (uint32_t i = 0; i < c; ++i) {
-    if ((e = launch_update(a, st))) return e;
-    L += a.n_upd_tiles ? 1 : 0;
-    if (any_csr) {
-      if ((e = launch_push(a, s.push_blocks, st))) return e;
-      L++;
-    }
-    if ((e = launch_pull_thread(a, st))) return e;
-    L += a.n_pull_tiles ? 1 : 0;
-    if ((e = launch_pull_warp(a, st))) return e;
-    L += a.n_pull_items ? 1 : 0;
-    if ((e = launch_advance(a, st))) return e;
+  if (s.cfg.exec_mode == SGB_EXEC_PERSISTENT) {
+    if ((e = cudaMemsetAsync(a.bar, 0, sizeof(unsigned long long), st))) return e;
+    if ((e = launch_persistent(a, c, s.persistent_blocks, st))) return e;
     L++;
+  } else {
+    for (uint32_t i = 0; i < c; ++i) {
+      if ((e = launch_update(a, st))) return e;
+      if ((e = launch_deliver(a, s.deliver_blocks, st))) return e;
+      L += 2;
+    }
   }
   if ((e = launch_chunk_end(a, st))) return e;
   L++;
@@ -528,47 +543,26 @@ static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nla
   return cudaSuccess;
 }
 
-static int get_graph(Sim& s, uint32_t c, cudaGraphExec_t* out, int64_t* nlaunch) {
-  auto it = s.graphs.find(c);
-  if (it != s.graphs.end()) {
-    // A graph launches the same kernels as the direct issue it was captured from.
-    bool any_csr = false;
-    for (const ProjDev& P : s.projs) any_csr |= P.mode == SGB_PROP_CSR && P.pre_count && P.post_count;
-    const StepArgs& a = s.args;
-    *out = it->second;
-    *nlaunch = 2 + (int64_t)c * ((a.n_upd_tiles ? 1 : 0) + (any_csr ? 1 : 0) +
-                                 (a.n_pull_tiles ? 1 : 0) + (a.n_pull_items ? 1 : 0) + 1);
-    return SGB_OK;
-  }
-  cudaGraph_t g;
-  SGB_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = issue_chunk(s, c, s.stream, nlaunch);
-  cudaError_t e2 = cudaStreamEndCapture(s.stream, &g);
-  if (e != cudaSuccess)
-    return set_error(SGB_ERR_CUDA, "capture of a %u-step chunk failed: %s", c, cudaGetErrorString(e));
-  if (e2 != cudaSuccess)
-    return set_error(SGB_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
-  cudaGraphExec_t ge;
-  e = cudaGraphInstantiate(&ge, g, 0);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return set_error(SGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
-  s.graphs[c] = ge;
-  *out = ge;
-  return SGB_OK;
-}
-
-static void drop_graphs(Sim& s) {
-  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
-  s.graphs.clear();
-}
-
 static int launch_chunk(Sim& s, uint32_t c) {
   int64_t L = 0;
   if (s.cfg.exec_mode == SGB_EXEC_GRAPH) {
-    cudaGraphExec_t ge;
-    int rc = get_graph(s, c, &ge, &L);
-    if (rc) return rc;
-    SGB_CUDA(cudaGraphLaunch(ge, s.stream));
+    auto it = s.graphs.find(c);
+    if (it == s.graphs.end()) {
+      cudaGraph_t g;
+      SGB_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = issue_chunk(s, c, s.stream, &L);
+      cudaError_t e2 = cudaStreamEndCapture(s.stream, &g);
+      if (e != cudaSuccess)
+        return set_error(SGB_ERR_CUDA, "capture of a %u-step chunk failed: %s", c, cudaGetErrorString(e));
+      if (e2 != cudaSuccess) return set_error(SGB_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
+      cudaGraphExec_t ge;
+      e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return set_error(SGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+      it = s.graphs.emplace(c, ge).first;
+    }
+    SGB_CUDA(cudaGraphLaunch(it->second, s.stream));
+    L = 2 + 2 * (int64_t)c;
   } else {
     cudaError_t e = issue_chunk(s, c, s.stream, &L);
     if (e != cudaSuccess) return set_error(SGB_ERR_CUDA, "step launch failed: %s", cudaGetErrorString(e));
@@ -601,7 +595,8 @@ int sim_sync(Sim& s) {
   int rc = check_device_error(s, &err);
   if (rc) return rc;
   SGB_CUDA(cudaMemsetAsync(&s.args.ctl->error, 0, 4, s.stream));
-  if (err & kErrBarrierTimeout) return set_error(SGB_ERR_DEVICE, "a device-side wait hit its limit");
+  if (err & kErrBarrierTimeout)
+    return set_error(SGB_ERR_DEVICE, "a device-side grid barrier hit its wait limit; reset the handle");
   return SGB_OK;
 }
 
@@ -643,7 +638,7 @@ int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int
               break;
             }
             const uint32_t pid = s.h_raster[q];
-            // Segment of the padded id by binary search over bases.
+            // Segment of the padded id by binary search over segment bases.
             size_t lo = 0, hi = nseg;
             while (hi - lo > 1) {
               const size_t mid = (lo + hi) / 2;
@@ -662,7 +657,8 @@ int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int
   int rc = check_device_error(s, &err);
   if (rc) return rc;
   SGB_CUDA(cudaMemsetAsync(&s.args.ctl->error, 0, 4, s.stream));
-  if (err & kErrBarrierTimeout) return set_error(SGB_ERR_DEVICE, "a device-side wait hit its limit");
+  if (err & kErrBarrierTimeout)
+    return set_error(SGB_ERR_DEVICE, "a device-side grid barrier hit its wait limit; reset the handle");
   if (overflow || (want_raster && (err & kErrRasterOverflow)))
     return set_error(SGB_ERR_OVERFLOW, "raster buffer too small; counts and state are intact");
   return SGB_OK;
@@ -680,10 +676,13 @@ int sim_set_rates(Sim& s, int32_t net, int32_t n, const float* rates) {
     p.rate_hz = rates[s.src_idx[k]];
     fill_source(s.srcs[k], p, s.cfg.dt_ms);
   }
-  if (!s.srcs.empty())
-    SGB_CUDA(cudaMemcpyAsync((void*)s.args.srcs, s.srcs.data(), s.srcs.size() * sizeof(SrcDev),
+  if (!s.srcs.empty()) {
+    // The pinned staging copy is reused only after the previous upload ended.
+    SGB_CUDA(cudaStreamSynchronize(s.stream));
+    memcpy(s.h_srcs, s.srcs.data(), s.srcs.size() * sizeof(SrcDev));
+    SGB_CUDA(cudaMemcpyAsync((void*)s.args.srcs, s.h_srcs, s.srcs.size() * sizeof(SrcDev),
                              cudaMemcpyHostToDevice, s.stream));
-  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  }
   return SGB_OK;
 }
 
@@ -736,23 +735,6 @@ int sim_totals(Sim& s, double* totals) {
   return SGB_OK;
 }
 
-static int upload_modes(Sim& s) {
-  std::vector<PullTile> tiles;
-  std::vector<PullItem> items;
-  rebuild_work_lists(s, tiles, items);
-  StepArgs& a = s.args;
-  SGB_CUDA(cudaMemcpyAsync((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice, s.stream));
-  if (!tiles.empty())
-    SGB_CUDA(cudaMemcpyAsync((void*)a.pull_tiles, tiles.data(), tiles.size() * sizeof(PullTile), cudaMemcpyHostToDevice, s.stream));
-  if (!items.empty())
-    SGB_CUDA(cudaMemcpyAsync((void*)a.pull_items, items.data(), items.size() * sizeof(PullItem), cudaMemcpyHostToDevice, s.stream));
-  SGB_CUDA(cudaStreamSynchronize(s.stream));
-  a.n_pull_tiles = (uint32_t)tiles.size();
-  a.n_pull_items = (uint32_t)items.size();
-  drop_graphs(s);
-  return SGB_OK;
-}
-
 int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
   if (net < 0 || net >= (int32_t)s.nets.size()) return set_error(SGB_ERR_ARG, "net %d out of range", net);
   if (proj < 0 || proj >= (int32_t)s.nets[net].projs.size())
@@ -765,6 +747,8 @@ int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
 int sim_set_stream(Sim& s, cudaStream_t st) {
   SGB_CUDA(cudaStreamSynchronize(s.stream));
   s.stream = st ? st : s.own_stream;
+  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
+  s.graphs.clear();
   return SGB_OK;
 }
 
@@ -773,66 +757,49 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   return set_error(SGB_ERR_UNSUPPORTED, "autotuner not available in this build");
 }
 
-// Instrumented run: the step loop with plain launches, each kernel class
-// bracketed by CUDA events on the handle's stream, synchronised per step so
-// the per-step spike and delivery counters can be read.
+// Instrumented run: the per-step kernels launched one by one, each bracketed
+// by CUDA events on the handle's stream, synchronised per step so that the
+// spike and delivery counters of every step can be read.
 int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t* launches) {
   if (n_steps < 1) return set_error(SGB_ERR_ARG, "n_steps must be >= 1");
   constexpr int K = SGB_KCLASS_COUNT;
   const StepArgs& a = s.args;
   const double W = s.bf16 ? 2.0 : 4.0;
-  // Static bytes per launch: update and the two dense pulls.
+  // Algorithmic bytes: update = state 16 B read + 16 B write + ring 8 B per
+  // LIF cell, mask 4 B per input cell, 4 B per bitmap word; deliver = per
+  // walked push synapse 4 B word + W weight + 8 B atomic, per spike 4 B list +
+  // 8 B row offsets, per dense ELL entry 4 + W B plus 8 B per post.
   double upd_bytes = (double)a.n_words * 4.0;
   for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 40.0 * d.count : 4.0 * d.count;
-  double pt_bytes = 0, pw_bytes = 0;
-  for (const ProjDev& P : s.projs) {
-    if (P.mode != SGB_PROP_ELL || !P.ell_K) continue;
-    const double b = (double)P.post_count * P.ell_K * (4.0 + W) + (double)P.post_count * 8.0;
-    (P.ell_rowmajor ? pw_bytes : pt_bytes) += b;
-  }
-  bool any_csr = false;
-  for (const ProjDev& P : s.projs) any_csr |= P.mode == SGB_PROP_CSR && P.pre_count && P.post_count;
+  double pull_bytes = 0;
+  for (const ProjDev& P : s.projs)
+    if (P.mode == SGB_PROP_ELL && P.ell_K)
+      pull_bytes += (double)P.post_count * P.ell_K * (4.0 + W) + (double)P.post_count * 8.0;
   cudaEvent_t ev[2 * K];
   for (auto& e : ev) SGB_CUDA(cudaEventCreate(&e));
   double tot_ms[K] = {0}, tot_bytes[K] = {0};
   int64_t nl[K] = {0};
   Ctl before, after;
   int32_t done = 0;
-  int rc = SGB_OK;
-  while (done < n_steps && rc == SGB_OK) {
+  while (done < n_steps) {
     const uint32_t c = (uint32_t)std::min<int64_t>(s.chunk, n_steps - done);
     SGB_CUDA(cudaMemsetAsync(a.counts, 0, (size_t)c * a.n_segs * 4, s.stream));
     SGB_CUDA(launch_chunk_begin(a, s.stream));
     for (uint32_t i = 0; i < c; ++i) {
       SGB_CUDA(cudaMemcpyAsync(&before, a.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream));
-      bool ran[K] = {false, false, false, false, false};
-      auto timed = [&](int k, cudaError_t (*fn)(const StepArgs&, cudaStream_t), bool on) -> cudaError_t {
-        if (!on) return cudaSuccess;
-        cudaEventRecord(ev[2 * k], s.stream);
-        cudaError_t e = fn(a, s.stream);
-        cudaEventRecord(ev[2 * k + 1], s.stream);
-        ran[k] = true;
-        return e;
-      };
-      cudaError_t e = timed(0, launch_update, a.n_upd_tiles > 0);
-      if (!e && any_csr) {
-        cudaEventRecord(ev[2], s.stream);
-        e = launch_push(a, s.push_blocks, s.stream);
-        cudaEventRecord(ev[3], s.stream);
-        ran[1] = true;
-      }
-      if (!e) e = timed(2, launch_pull_thread, a.n_pull_tiles > 0);
-      if (!e) e = timed(3, launch_pull_warp, a.n_pull_items > 0);
-      if (!e) e = timed(4, launch_advance, true);
-      if (e) return set_error(SGB_ERR_CUDA, "profiled launch failed: %s", cudaGetErrorString(e));
+      SGB_CUDA(cudaEventRecord(ev[0], s.stream));
+      SGB_CUDA(launch_update(a, s.stream));
+      SGB_CUDA(cudaEventRecord(ev[1], s.stream));
+      SGB_CUDA(cudaEventRecord(ev[2], s.stream));
+      SGB_CUDA(launch_deliver(a, s.deliver_blocks, s.stream));
+      SGB_CUDA(cudaEventRecord(ev[3], s.stream));
       SGB_CUDA(cudaMemcpyAsync(&after, a.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream));
       SGB_CUDA(cudaStreamSynchronize(s.stream));
       const double spikes = (double)after.active_count[before.step & 1];
-      const double deliv = (double)(after.delivered - before.delivered);
-      const double step_bytes[K] = {upd_bytes + spikes * 4.0, deliv * (12.0 + W) + spikes * 12.0,
-                                    pt_bytes, pw_bytes, 64.0};
+      const double walked = (double)(after.delivered - before.delivered);
+      const double step_bytes[K] = {upd_bytes + spikes * 4.0,
+                                    walked * (12.0 + W) + spikes * 12.0 + pull_bytes};
       for (int k = 0; k < K; ++k) {
-        if (!ran[k]) continue;
         float ms = 0.f;
         SGB_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
         tot_ms[k] += ms;
@@ -852,7 +819,7 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
     if (bytes) bytes[k] = nl[k] ? tot_bytes[k] / (double)nl[k] : 0.0;
     if (launches) launches[k] = nl[k];
   }
-  return rc;
+  return SGB_OK;
 }
 
 }  // namespace sgb

@@ -14,12 +14,11 @@ namespace sgb {
 struct ProjTables {
   int32_t net = 0, proj = 0;
   uint32_t pre_seg = 0, post_seg = 0;
+  int32_t scale_bits = 0;  // of the post segment's accumulator
   int64_t nnz = 0;
   uint32_t ell_K = 0;
   bool ell_rowmajor = false;
-  int32_t max_out = 0;
-  // Device sub-allocations inside the table pool.
-  size_t off_csr_row = 0, off_csr_syn = 0, off_csr_w = 0, off_ell_syn = 0, off_ell_w = 0;
+  size_t off_ell_syn = 0, off_ell_w = 0;  // offsets inside the ELL pool
 };
 
 struct Sim {
@@ -35,7 +34,6 @@ struct Sim {
   std::vector<int32_t> seg_net, seg_pop;
   std::vector<int32_t> net_seg0;      // first segment of each net
   std::vector<int32_t> net_proj0;     // first projection of each net
-  std::vector<int32_t> net_src0;      // first source of each net (in srcs)
   std::vector<ProjDev> projs;
   std::vector<ProjTables> ptab;
   std::vector<SrcDev> srcs;
@@ -46,12 +44,16 @@ struct Sim {
   bool bf16 = false;
 
   // Device memory.
-  void* d_pool = nullptr;   // synapse tables
-  size_t pool_bytes = 0;
-  void* d_misc = nullptr;   // everything else
+  void* d_ell = nullptr;    // per-projection ELL tables
+  size_t ell_bytes = 0;
+  void* d_push = nullptr;   // merged push table (capacity: every synapse)
+  size_t push_bytes = 0;
+  void* d_misc = nullptr;   // state, ring, history, lists, descriptors
   size_t misc_bytes = 0;
   StepArgs args{};
-  int push_blocks = 0;
+  int deliver_blocks = 0;
+  int persistent_blocks = 0;
+  SrcDev* h_srcs = nullptr;  // pinned staging of the source table
 
   // Host staging for outputs.
   uint32_t* h_counts = nullptr;
@@ -60,7 +62,6 @@ struct Sim {
 
   std::map<uint32_t, cudaGraphExec_t> graphs;  // by chunk length
   int64_t launches = 0;
-  int64_t launches_per_step = 0;
 
   ~Sim();
 };
@@ -81,9 +82,9 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path);
 int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t* launches);
 int sim_set_stream(Sim& s, cudaStream_t st);
 
-// Network handle behind the C ABI.
 }  // namespace sgb
 
+// Handles behind the C ABI.
 struct sgb_net {
   sgb::Network net;
 };

@@ -1,24 +1,25 @@
 // Step kernels of the scaffold simulation hot path (sm_103a).
 //
-// One exchange step t runs, in stream order:
-//   k_update      every cell: INPUT cells draw their Philox Poisson / periodic
-//                 stimulus (reference InputStimulation, UserInputFunctions.cu:
-//                 86-120); LIF cells consume ring slot t and integrate
-//                 `substeps` Euler substeps (reference update_lif_ch,
-//                 Simulation_header.cu:305-381).  Spikes leave the kernel as
-//                 a bitmap word per warp (ballot), a compacted active list
-//                 (ballot + popc + one atomic per warp) and per-segment counts.
-//   k_push_csr    event-driven delivery: one warp per spiking cell walks the
-//                 cell's pre-major rows and adds fixed-point weights into
-//                 ring slot t + delay of each target.
-//   k_pull_*      dense delivery for projections in ELL mode: each post cell
-//                 gathers the spike bits of its in-row from the bitmap of
-//                 step t + 1 - delay and adds the sum into ring slot t + 1
-//                 (the reference's pull, Simulation_header.cu:83-139, with
-//                 the delay applied on read as at GPUScaffoldSimulation.cu:735).
-//   k_advance     step bookkeeping (ring slot, history row, buffer parity).
-// The ring holds int32 fixed-point sums, so CSR and ELL delivery, any launch
-// order and any number of instances give bit-identical conductances.
+// One exchange step t consists of two grid-wide phases:
+//   update   every cell, one warp per 32-cell word: INPUT cells draw their
+//            Philox Poisson / periodic stimulus (reference InputStimulation,
+//            UserInputFunctions.cu:86-120); LIF cells consume ring slot t and
+//            integrate `substeps` Euler substeps (reference update_lif_ch,
+//            Simulation_header.cu:305-381).  Spikes leave as a bitmap word
+//            per warp (ballot), a compacted active list (ballot + popc + one
+//            atomic per warp) and per-segment counts.
+//   deliver  event-driven push: one warp per spiking cell walks the cell's
+//            row of the push table and adds fixed-point weights into ring
+//            slot t + delay of each target; dense pull for projections in ELL
+//            mode: each post cell gathers the spike bits of its in-row from the
+//            bitmap of step t + 1 - delay and adds the sum into ring slot t + 1
+//            (the reference's pull, Simulation_header.cu:83-139, with the delay
+//            applied on read as at GPUScaffoldSimulation.cu:735).
+// Two drivers run these phases: per-step kernels (replayed from a CUDA graph;
+// kernel boundaries order the phases) and one persistent cooperative kernel
+// per chunk of steps (a bounded grid barrier orders them).  The ring holds
+// int32 fixed-point sums, so push and pull delivery, any launch order and any
+// number of instances give bit-identical conductances.
 #include <stdint.h>
 
 #include "sgb_device.h"
@@ -30,13 +31,18 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ float load_weight(const void* w, uint32_t q, bool bf16) {
-  if (bf16) return __uint_as_float(((uint32_t)((const uint16_t*)w)[q]) << 16);
-  return ((const float*)w)[q];
-}
+// Step indices shared by every phase of one step.
+struct StepIdx {
+  unsigned long long t;
+  uint32_t slot;  // t % ring_slots
+  uint32_t hrow;  // t % hist_rows
+  uint32_t rel;   // step index within the chunk
+};
 
-__device__ __forceinline__ int to_fixed(float w, float scale) {
-  return __float2int_rn(__fmul_rn(w, scale));
+template <bool BF16>
+__device__ __forceinline__ float load_weight(const void* w, uint32_t q) {
+  if (BF16) return __uint_as_float(((uint32_t)__ldg((const unsigned short*)w + q)) << 16);
+  return __ldg((const float*)w + q);
 }
 
 __device__ __forceinline__ bool window_on(const SrcDev& s, int64_t k) {
@@ -115,52 +121,46 @@ __device__ __forceinline__ bool lif_update(const SegDev& sd, int substeps, float
   return spk;
 }
 
-__global__ void k_chunk_begin(StepArgs a) {
-  a.ctl->t_rel = 0;
-  a.ctl->raster_count = 0;
-  a.raster_off[0] = 0;
-}
-
-__global__ void __launch_bounds__(kUpdateTile) k_update(StepArgs a) {
-  const UpdTile tile = a.upd_tiles[blockIdx.x];
-  const SegDev& sd = a.segs[tile.seg];
-  const uint32_t i = tile.start + threadIdx.x;
-  const uint32_t i0 = i & ~31u;
-  if (i0 - sd.base >= sd.count) return;  // whole warp past the segment end
+// ---- phase 1: one warp updates the 32 cells of word w --------------------------
+// Cross-block data (ring slots written by other SMs' atomics, counters) is read
+// with ld.global.cg so a persistent kernel never sees a stale L1 line.
+__device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t seg = __ldg(a.seg_of_word + w);
+  const SegDev& sd = a.segs[seg];
+  const uint32_t i = (w << 5) + lane;
   const uint32_t local = i - sd.base;
   const bool valid = local < sd.count;
-  Ctl* ctl = a.ctl;
-  const unsigned long long t = ctl->step;
   bool fired = false;
   if (valid) {
     if (sd.kind == kSegInput) {
-      const uint32_t mask = a.src_mask[i];
-      if (mask) fired = input_fire(a, sd, local, mask, t);
+      const uint32_t mask = __ldg(a.src_mask + i);
+      if (mask) fired = input_fire(a, sd, local, mask, ix.t);
     } else {
-      int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ctl->ring_slot * a.n_pad + i;
-      const int2 acc = *rp;
-      if (acc.x | acc.y) *rp = make_int2(0, 0);
+      int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i;
+      const int2 acc = __ldcg(rp);
+      if (acc.x | acc.y) __stcg(rp, make_int2(0, 0));
       float4 st = a.state[i];
       fired = lif_update(sd, a.substeps, st, acc);
       a.state[i] = st;
     }
   }
   const uint32_t ballot = __ballot_sync(kFull, fired);
-  const uint32_t lane = threadIdx.x & 31u;
-  if (lane == 0) a.hist[(size_t)ctl->hist_row * a.n_words + (i >> 5)] = ballot;
+  if (lane == 0) __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, ballot);
   if (ballot == 0) return;
   const uint32_t n = __popc(ballot);
   const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
-  const uint32_t ev = __reduce_add_sync(kFull, fired ? a.outdeg[i] : 0u);
+  const uint32_t ev = __reduce_add_sync(kFull, fired ? __ldg(a.outdeg + i) : 0u);
   uint32_t off = 0, roff = 0;
+  Ctl* ctl = a.ctl;
   if (lane == 0) {
-    off = atomicAdd(&ctl->active_count[t & 1], n);
-    atomicAdd(&a.counts[(size_t)ctl->t_rel * a.n_segs + tile.seg], n);
+    off = atomicAdd(&ctl->active_count[ix.t & 1], n);
+    atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], n);
     if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
     if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
   }
   off = __shfl_sync(kFull, off, 0);
-  if (fired) a.active[(size_t)(t & 1) * a.n_pad + off + rank] = i;
+  if (fired) __stcg(a.active + (size_t)(ix.t & 1) * a.n_pad + off + rank, i);
   if (a.raster_cap) {
     roff = __shfl_sync(kFull, roff, 0);
     if (fired) {
@@ -172,127 +172,234 @@ __global__ void __launch_bounds__(kUpdateTile) k_update(StepArgs a) {
   }
 }
 
-// One warp per spiking cell; lanes stride over the cell's CSR row so that
-// synapse words and weights are read as coalesced 128-byte lines.
+// ---- phase 2: deliveries ------------------------------------------------------
+// One warp walks the push-table row of spiking cell j (coalesced 128-byte
+// lines); returns the row length (lane 0 accounts it).
 template <bool BF16>
-__global__ void __launch_bounds__(256) k_push_csr(StepArgs a) {
-  Ctl* ctl = a.ctl;
-  const unsigned long long t = ctl->step;
-  const uint32_t n_active = ctl->active_count[t & 1];
-  const uint32_t* list = a.active + (size_t)(t & 1) * a.n_pad;
-  const uint32_t slot0 = ctl->ring_slot;
+__device__ __forceinline__ uint32_t push_spike(const StepArgs& a, uint32_t j, uint32_t slot0) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t e = warp; e < n_active; e += n_warps) {
-    const uint32_t j = list[e];
-    const SegDev& sd = a.segs[a.seg_of_word[j >> 5]];
-    const uint32_t local = j - sd.base;
-    for (uint32_t o = 0; o < sd.out_count; ++o) {
-      const ProjDev& P = a.projs[a.out_list[sd.out_first + o]];
-      if (P.mode != SGB_PROP_CSR) continue;
-      const uint32_t r0 = P.csr_row[local], r1 = P.csr_row[local + 1];
-      if (lane == 0 && r1 > r0) atomicAdd(&a.ctl->delivered, (unsigned long long)(r1 - r0));
-      for (uint32_t q = r0 + lane; q < r1; q += 32) {
-        const uint32_t wd = P.csr_syn[q];
-        const uint32_t d = wd >> kIndexBits;
-        uint32_t slot = slot0 + d;
-        if (slot >= a.ring_slots) slot -= a.ring_slots;
-        const int fx = to_fixed(load_weight(P.csr_w, q, BF16), P.scale);
-        atomicAdd(a.ring + (((size_t)slot * a.n_pad + P.post_base + (wd & kIndexMask)) << 1) +
-                      P.channel,
-                  fx);
-      }
-    }
+  const uint32_t r0 = __ldg(a.push_row + j), r1 = __ldg(a.push_row + j + 1);
+  for (uint32_t q = r0 + lane; q < r1; q += 32) {
+    const uint32_t wd = __ldg(a.push_syn + q);
+    const int fx = __float2int_rn(load_weight<BF16>(a.push_w, q));
+    uint32_t slot = slot0 + ((wd >> kPushPostBits) & 15u);
+    if (slot >= a.ring_slots) slot -= a.ring_slots;
+    atomicAdd(a.ring + (((size_t)slot * a.n_pad + (wd & kPushPostMask)) << 1) + (wd >> 31), fx);
   }
+  return r1 - r0;
 }
 
-__device__ __forceinline__ uint32_t spike_bit(const StepArgs& a, uint32_t hist_row_t,
+__device__ __forceinline__ uint32_t spike_bit(const StepArgs& a, uint32_t hrow,
                                               uint32_t pre_global, uint32_t d) {
-  uint32_t row = hist_row_t + 1u + a.hist_rows - d;  // row of step t + 1 - d
-  row %= a.hist_rows;
-  return (__ldg(a.hist + (size_t)row * a.n_words + (pre_global >> 5)) >> (pre_global & 31u)) & 1u;
+  uint32_t row = hrow + 1u + a.hist_rows - d;  // row of step t + 1 - d
+  if (row >= a.hist_rows) row -= a.hist_rows;
+  if (row >= a.hist_rows) row -= a.hist_rows;
+  return (__ldcg(a.hist + (size_t)row * a.n_words + (pre_global >> 5)) >> (pre_global & 31u)) & 1u;
 }
 
-// Column-major ELL: one thread per post cell, ELL column k of all posts is
-// contiguous, so a warp reads consecutive words per k.
+// Column-major ELL: each lane owns one post cell; column k of all posts is
+// contiguous, so the warp reads consecutive words per k.
 template <bool BF16>
-__global__ void __launch_bounds__(kPullThreadTile) k_pull_thread(StepArgs a) {
-  const PullTile tile = a.pull_tiles[blockIdx.x];
+__device__ __forceinline__ void pull_tile(const StepArgs& a, const PullTile& tile,
+                                          const StepIdx& ix) {
   const ProjDev& P = a.projs[tile.proj];
-  if (P.mode != SGB_PROP_ELL) return;
-  const uint32_t p = tile.post_start + threadIdx.x;
+  const uint32_t p = tile.post_start + (threadIdx.x & 31u);
   if (p >= P.post_count) return;
-  const Ctl* ctl = a.ctl;
-  const uint32_t hrow = ctl->hist_row;
   int acc = 0;
   for (uint32_t k = 0; k < P.ell_K; ++k) {
     const uint32_t q = k * P.post_count + p;
     const uint32_t wd = __ldg(P.ell_syn + q);
     if (wd == kEllPad) break;  // padding is at the end of each row
-    if (spike_bit(a, hrow, P.pre_base + (wd & kIndexMask), wd >> kIndexBits))
-      acc += to_fixed(load_weight(P.ell_w, q, BF16), P.scale);
+    if (spike_bit(a, ix.hrow, P.pre_base + (wd & kIndexMask), wd >> kIndexBits))
+      acc += __float2int_rn(load_weight<BF16>(P.ell_w, q));
   }
   if (acc) {
-    uint32_t slot = ctl->ring_slot + 1u;
+    uint32_t slot = ix.slot + 1u;
     if (slot >= a.ring_slots) slot -= a.ring_slots;
     atomicAdd(a.ring + (((size_t)slot * a.n_pad + P.post_base + p) << 1) + P.channel, acc);
   }
 }
 
-// Row-major ELL for wide rows: one warp per (post, chunk of kPullWarpChunk).
+// Row-major ELL for wide rows: the warp strides over one row chunk.
 template <bool BF16>
-__global__ void __launch_bounds__(256) k_pull_warp(StepArgs a) {
-  const uint32_t item_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (item_id >= a.n_pull_items) return;
-  const PullItem it = a.pull_items[item_id];
+__device__ __forceinline__ void pull_item(const StepArgs& a, const PullItem& it,
+                                          const StepIdx& ix) {
   const ProjDev& P = a.projs[it.proj];
-  if (P.mode != SGB_PROP_ELL) return;
   const uint32_t lane = threadIdx.x & 31u;
-  const Ctl* ctl = a.ctl;
-  const uint32_t hrow = ctl->hist_row;
   const uint32_t k1 = min(it.k0 + (uint32_t)kPullWarpChunk, P.ell_K);
   const size_t row = (size_t)it.post * P.ell_K;
   int acc = 0;
   for (uint32_t k = it.k0 + lane; k < k1; k += 32) {
     const uint32_t wd = __ldg(P.ell_syn + row + k);
-    if (wd != kEllPad &&
-        spike_bit(a, hrow, P.pre_base + (wd & kIndexMask), wd >> kIndexBits))
-      acc += to_fixed(load_weight(P.ell_w, (uint32_t)(row + k), BF16), P.scale);
+    if (wd != kEllPad && spike_bit(a, ix.hrow, P.pre_base + (wd & kIndexMask), wd >> kIndexBits))
+      acc += __float2int_rn(load_weight<BF16>(P.ell_w, (uint32_t)(row + k)));
   }
   acc = __reduce_add_sync(kFull, acc);
   if (lane == 0 && acc) {
-    uint32_t slot = ctl->ring_slot + 1u;
+    uint32_t slot = ix.slot + 1u;
     if (slot >= a.ring_slots) slot -= a.ring_slots;
     atomicAdd(a.ring + (((size_t)slot * a.n_pad + P.post_base + it.post) << 1) + P.channel, acc);
   }
 }
 
-__global__ void k_advance(StepArgs a) {
+// Warp-level dispatch of delivery unit u: spikes first, then ELL tiles and items.
+template <bool BF16>
+__device__ __forceinline__ uint32_t deliver_unit(const StepArgs& a, uint32_t u, uint32_t n_act,
+                                                 const uint32_t* list, const StepIdx& ix) {
+  if (u < n_act) return push_spike<BF16>(a, __ldcg(list + u), ix.slot);
+  u -= n_act;
+  if (u < a.n_pull_tiles) {
+    pull_tile<BF16>(a, a.pull_tiles[u], ix);
+    return 0;
+  }
+  pull_item<BF16>(a, a.pull_items[u - a.n_pull_tiles], ix);
+  return 0;
+}
+
+__device__ __forceinline__ StepIdx step_of(const Ctl* ctl) {
+  StepIdx ix;
+  ix.t = ctl->step;
+  ix.slot = ctl->ring_slot;
+  ix.hrow = ctl->hist_row;
+  ix.rel = ctl->t_rel;
+  return ix;
+}
+
+// ---- per-step kernels (CUDA-graph driver) ----------------------------------
+__global__ void k_chunk_begin(StepArgs a) {
+  a.ctl->t_rel = 0;
+  a.ctl->raster_count = 0;
+  a.raster_off[0] = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_update(StepArgs a) {
+  const uint32_t u = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  if (u >= a.n_upd_words) return;
+  const StepIdx ix = step_of(a.ctl);
+  update_word(a, __ldg(a.upd_words + u), ix);
+}
+
+// Delivery of step t; the last block to finish also advances the step
+// (ring slot, history row, buffer parity, raster offsets).
+template <bool BF16>
+__global__ void __launch_bounds__(kBlock) k_deliver(StepArgs a) {
   Ctl* ctl = a.ctl;
-  const unsigned long long t = ctl->step + 1ull;
-  ctl->step = t;
-  ctl->ring_slot = ctl->ring_slot + 1u == a.ring_slots ? 0u : ctl->ring_slot + 1u;
-  ctl->hist_row = ctl->hist_row + 1u == a.hist_rows ? 0u : ctl->hist_row + 1u;
-  ctl->active_count[t & 1] = 0;
-  const uint32_t r = ++ctl->t_rel;
-  a.raster_off[r] = ctl->raster_count;
+  const StepIdx ix = step_of(ctl);
+  const uint32_t n_act = a.any_push ? ctl->active_count[ix.t & 1] : 0u;
+  const uint32_t* list = a.active + (size_t)(ix.t & 1) * a.n_pad;
+  const uint32_t n_units = n_act + a.n_pull_tiles + a.n_pull_items;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  uint32_t walked = 0;
+  for (uint32_t u = (blockIdx.x * kBlock + threadIdx.x) >> 5; u < n_units; u += nw)
+    walked += deliver_unit<BF16>(a, u, n_act, list, ix);
+  if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
+  // Step bookkeeping by the last block to arrive.
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(&ctl->barrier_gen, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    ctl->barrier_gen = 0;
+    const unsigned long long t = ix.t + 1ull;
+    ctl->step = t;
+    ctl->ring_slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+    ctl->hist_row = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+    ctl->active_count[t & 1] = 0;
+    ctl->t_rel = ix.rel + 1u;
+    a.raster_off[ix.rel + 1u] = ctl->raster_count;
+  }
 }
 
 // Per-segment spike totals of the chunk, folded into the FP64 accumulators.
-__global__ void __launch_bounds__(256) k_chunk_end(StepArgs a) {
+__global__ void __launch_bounds__(kBlock) k_chunk_end(StepArgs a) {
   const uint32_t seg = blockIdx.x;
   const uint32_t steps = a.ctl->t_rel;
   unsigned long long s = 0;
   for (uint32_t r = threadIdx.x; r < steps; r += blockDim.x) s += a.counts[(size_t)r * a.n_segs + seg];
   for (int o = 16; o; o >>= 1) s += __shfl_down_sync(kFull, s, o);
-  __shared__ unsigned long long part[8];
+  __shared__ unsigned long long part[kBlock / 32];
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long tot = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w];
+    for (int w = 0; w < kBlock / 32; ++w) tot += part[w];
     a.totals[seg] += (double)tot;
+  }
+}
+
+// ---- persistent driver ----------------------------------------------------------
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier over co-resident blocks (cooperative launch).  Thread 0
+// of each block publishes its block's writes (fence), arrives on a counter,
+// then waits -- at most kBarrierSpinLimit polls -- for all blocks of this
+// round.  On timeout it records kErrBarrierTimeout; every block then returns
+// at its next barrier, so the kernel always ends.
+__device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long long& target) {
+  __shared__ int abort_flag;
+  __syncthreads();
+  target += gridDim.x;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    atomicAdd(a.bar, 1ull);
+    uint32_t it = 0;
+    while (ld_acquire(a.bar) < target) {
+      if (++it > kBarrierSpinLimit || (it % 4096 == 0 && (__ldcg(&a.ctl->error) & kErrBarrierTimeout))) {
+        atomicOr(&a.ctl->error, kErrBarrierTimeout);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    abort_flag = !ok;
+  }
+  __syncthreads();
+  return !abort_flag;
+}
+
+template <bool BF16>
+__global__ void __launch_bounds__(kBlock) k_persistent(StepArgs a, uint32_t n_steps) {
+  Ctl* ctl = a.ctl;
+  StepIdx ix = step_of(ctl);
+  const unsigned long long t0 = ix.t;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long target = 0;
+  uint32_t walked = 0;
+  for (uint32_t s = 0; s < n_steps; ++s) {
+    ix.t = t0 + s;
+    ix.rel = s;
+    // Buffer of step t + 1: its last reader was the delivery of step t - 1.
+    if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
+    for (uint32_t u = gw; u < a.n_upd_words; u += nw) update_word(a, __ldg(a.upd_words + u), ix);
+    if (!grid_barrier(a, target)) return;
+    if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
+    const uint32_t n_act = a.any_push ? __ldcg(&ctl->active_count[ix.t & 1]) : 0u;
+    const uint32_t* list = a.active + (size_t)(ix.t & 1) * a.n_pad;
+    const uint32_t n_units = n_act + a.n_pull_tiles + a.n_pull_items;
+    for (uint32_t u = gw; u < n_units; u += nw) walked += deliver_unit<BF16>(a, u, n_act, list, ix);
+    if (!grid_barrier(a, target)) return;
+    ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+    ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+  }
+  if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
+  if (leader) {
+    ctl->step = t0 + n_steps;
+    ctl->ring_slot = ix.slot;
+    ctl->hist_row = ix.hrow;
+    ctl->t_rel = n_steps;
   }
 }
 
@@ -304,48 +411,40 @@ cudaError_t launch_chunk_begin(const StepArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_update(const StepArgs& a, cudaStream_t s) {
-  if (!a.n_upd_tiles) return cudaSuccess;
-  k_update<<<a.n_upd_tiles, kUpdateTile, 0, s>>>(a);
+  if (!a.n_upd_words) return cudaSuccess;
+  k_update<<<(a.n_upd_words + kBlock / 32 - 1) / (kBlock / 32), kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_push(const StepArgs& a, int blocks, cudaStream_t s) {
-  if (blocks <= 0) return cudaSuccess;
+cudaError_t launch_deliver(const StepArgs& a, int blocks, cudaStream_t s) {
   if (a.bf16)
-    k_push_csr<true><<<blocks, 256, 0, s>>>(a);
+    k_deliver<true><<<blocks, kBlock, 0, s>>>(a);
   else
-    k_push_csr<false><<<blocks, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pull_thread(const StepArgs& a, cudaStream_t s) {
-  if (!a.n_pull_tiles) return cudaSuccess;
-  if (a.bf16)
-    k_pull_thread<true><<<a.n_pull_tiles, kPullThreadTile, 0, s>>>(a);
-  else
-    k_pull_thread<false><<<a.n_pull_tiles, kPullThreadTile, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pull_warp(const StepArgs& a, cudaStream_t s) {
-  if (!a.n_pull_items) return cudaSuccess;
-  const unsigned blocks = (a.n_pull_items + 7u) / 8u;
-  if (a.bf16)
-    k_pull_warp<true><<<blocks, 256, 0, s>>>(a);
-  else
-    k_pull_warp<false><<<blocks, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_advance(const StepArgs& a, cudaStream_t s) {
-  k_advance<<<1, 1, 0, s>>>(a);
+    k_deliver<false><<<blocks, kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
   if (!a.n_segs) return cudaSuccess;
-  k_chunk_end<<<a.n_segs, 256, 0, s>>>(a);
+  k_chunk_end<<<a.n_segs, kBlock, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+int persistent_blocks_per_sm(bool bf16) {
+  int n = 0;
+  if (bf16)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true>, kBlock, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, kBlock, 0);
+  return n;
+}
+
+cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s) {
+  StepArgs args = a;
+  uint32_t n = n_steps;
+  void* params[] = {&args, &n};
+  const void* fn = a.bf16 ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kBlock), params, 0, s);
 }
 
 }  // namespace sgb

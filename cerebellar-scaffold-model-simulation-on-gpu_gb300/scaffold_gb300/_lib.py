@@ -22,7 +22,7 @@ PROP_AUTO, PROP_CSR, PROP_ELL = 0, 1, 2
 WEIGHT_FP32, WEIGHT_BF16 = 0, 1
 EXEC_GRAPH, EXEC_PERSISTENT, EXEC_STREAM = 0, 1, 2
 INPUT_POISSON, INPUT_PERIODIC = 0, 1
-KCLASS_COUNT = 5
+KCLASS_COUNT = 2
 
 
 class SgbError(RuntimeError):
@@ -34,7 +34,8 @@ class SgbError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [("dt_ms", C.c_double), ("substeps", C.c_int32), ("weight_type", C.c_int32),
                 ("exec_mode", C.c_int32), ("chunk_steps", C.c_int32), ("device", C.c_int32),
-                ("default_prop", C.c_int32), ("raster", C.c_int32), ("reserved", C.c_int32 * 9)]
+                ("default_prop", C.c_int32), ("raster", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("reserved", C.c_int32 * 8)]
 
 
 class InputParams(C.Structure):

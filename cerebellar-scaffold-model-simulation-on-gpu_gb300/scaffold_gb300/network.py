@@ -220,7 +220,7 @@ class Simulation:
     def __init__(self, nets: Sequence[Network], seeds: Sequence[int] | None = None, *,
                  dt_ms: float = 0.1, substeps: int = 1, weight_type: int = L.WEIGHT_FP32,
                  exec_mode: int = L.EXEC_GRAPH, chunk_steps: int = 1000, device: int = 0,
-                 default_prop: int = L.PROP_AUTO, raster: bool = False):
+                 default_prop: int = L.PROP_AUTO, raster: bool = False, blocks_per_sm: int = 0):
         cfg = L.Config()
         L.lib().sgb_config_init(C.byref(cfg))
         cfg.dt_ms = dt_ms
@@ -231,6 +231,7 @@ class Simulation:
         cfg.device = device
         cfg.default_prop = default_prop
         cfg.raster = 1 if raster else 0
+        cfg.blocks_per_sm = blocks_per_sm
         self.nets = list(nets)
         n = len(self.nets)
         arr = (C.c_void_p * n)(*[x.handle.value for x in self.nets])

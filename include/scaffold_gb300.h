@@ -87,7 +87,8 @@ typedef struct sgb_config {
   int32_t device;        /* CUDA device ordinal                                          */
   int32_t default_prop;  /* mode for projections added with SGB_PROP_AUTO                */
   int32_t raster;        /* 1: record every spike for sgb_sim_run's raster output        */
-  int32_t reserved[9];
+  int32_t blocks_per_sm; /* persistent driver: resident blocks per SM (0: 1)              */
+  int32_t reserved[8];
 } sgb_config;
 
 typedef struct sgb_input_params {
@@ -280,12 +281,12 @@ int sgb_sim_autotune(sgb_sim* sim, int32_t n_steps, const char* cache_path);
 /* Number of kernel launches issued so far (graph nodes count one each). */
 int sgb_sim_launch_count(const sgb_sim* sim, int64_t* launches);
 
-/* Instrumented run: advances n_steps with plain launches bracketed by CUDA
- * events on the handle's stream and returns, per kernel class (0 update,
- * 1 push, 2 pull_thread, 3 pull_warp, 4 advance), the mean device time per
- * launch in microseconds, the mean algorithmic bytes per launch, and the
- * number of launches. */
-#define SGB_KCLASS_COUNT 5
+/* Instrumented run: advances n_steps with the per-step kernels launched one by
+ * one, each bracketed by CUDA events on the handle's stream, and returns per
+ * kernel class (0 update, 1 deliver) the mean device time per launch in
+ * microseconds, the mean algorithmic bytes per launch, and the number of
+ * launches. */
+#define SGB_KCLASS_COUNT 2
 int sgb_sim_profile(sgb_sim* sim, int32_t n_steps, double* mean_us, double* bytes_per_launch,
                     int64_t* launches);
 
