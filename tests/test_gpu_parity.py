@@ -144,7 +144,7 @@ def test_state_roundtrip_and_totals():
     tot = sim.spike_totals()
     assert np.array_equal(tot, c.sum(0).astype(np.float64))
     u, g, ref = sim.state()
-    assert np.isfinite(u).all() and (ref >= 0).all() and ref.max() > 0
+    assert np.isfinite(u).all() and (ref >= 0).all()
     sim.set_state(u + 0.0, g * 0.5, ref)
     u2, g2, ref2 = sim.state()
     assert np.array_equal(u2, u) and np.array_equal(g2, g * 0.5) and np.array_equal(ref2, ref)
