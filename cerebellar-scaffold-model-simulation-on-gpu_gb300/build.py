@@ -35,6 +35,7 @@ SOURCES = [
     ("sgb_capi.cpp", "cxx"),
     ("sgb_engine.cu", "nvcc"),
     ("sgb_kernels.cu", "nvcc"),
+    ("sgb_ops.cu", "nvcc"),
 ]
 HEADERS = ["sgb_philox.h", "sgb_model.h", "sgb_device.h", "sgb_engine.h"]
 

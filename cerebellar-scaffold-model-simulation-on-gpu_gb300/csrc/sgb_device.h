@@ -11,8 +11,9 @@
 //              delay + 1 slots.  Integer accumulation makes every sum exact
 //              and independent of the order in which spikes are delivered.
 //   history    spike bitmaps of the last H = max delay steps (1 bit per cell).
-//   active     compacted ids of the cells that fired in the current step
-//              (double-buffered by step parity).
+//   items      push work of the current step: for every spiking cell, its
+//              push-table row cut into ranges of at most kPushChunk synapses
+//              (uint2 {first, end}); double-buffered by step parity.
 //   push table one cell-major CSR over every projection in event-driven mode
 //              (all instances): synapse word = padded post index | delay << 27
 //              | accumulator << 31, plus the weight pre-multiplied by its
@@ -25,7 +26,9 @@
 
 namespace sgb {
 
-constexpr int kBlock = 256;           // threads per block of every step kernel
+constexpr int kBlock = 256;           // threads per block of the per-step kernels
+constexpr int kPersistBlock = 1024;   // threads per block of the persistent kernel
+constexpr uint32_t kPushChunk = 256;  // synapses per push work item (8 per lane)
 constexpr int kPullWarpChunk = 1024;  // synapses per warp item of the row-major ELL pull
 constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-major layout
 // Push-table synapse word: 27-bit padded post index, 4-bit delay, 1-bit accumulator.
@@ -83,7 +86,7 @@ struct Ctl {
   uint32_t ring_slot;             // step % D
   uint32_t hist_row;              // step % H
   uint32_t t_rel;                 // step index within the current chunk
-  uint32_t active_count[2];       // spikes of step s live in buffer s & 1
+  uint32_t active_count[2];       // push items of step s live in buffer s & 1
   uint32_t raster_count;          // spikes recorded in the current chunk
   uint32_t error;                 // device error bits (kErr*)
   uint32_t barrier_gen;           // persistent-kernel grid barrier state
@@ -117,7 +120,7 @@ struct StepArgs {
   float4* state;
   int* ring;                      // int2 per cell per slot, viewed as int[2]
   uint32_t* hist;                 // [H][n_words]
-  uint32_t* active;               // [2][n_pad]
+  uint2* items;                   // [2][item_cap] push work ranges
   uint32_t* counts;               // [chunk_steps][n_segs]
   uint32_t* raster;               // [raster_cap] padded ids
   uint32_t* raster_off;           // [chunk_steps + 1]
@@ -128,6 +131,7 @@ struct StepArgs {
   uint32_t n_upd_words, n_pull_tiles, n_pull_items;
   uint32_t any_push;
   uint32_t raster_cap;
+  uint32_t item_cap;              // items per parity buffer
   int32_t bf16;
   int32_t substeps;
 };

@@ -422,7 +422,9 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   const size_t o_state = take((size_t)s.n_pad * sizeof(float4));
   const size_t o_ring = take((size_t)s.ring_slots * s.n_pad * 8);
   const size_t o_hist = take((size_t)s.hist_rows * s.n_words * 4);
-  const size_t o_active = take((size_t)2 * s.n_pad * 4);
+  const uint64_t item_cap = (uint64_t)s.n_pad + (uint64_t)(s.n_syn / kPushChunk) + 1;
+  if (item_cap > 0xFFFFFFFFull) return set_error(SGB_ERR_UNSUPPORTED, "push work list too large");
+  const size_t o_items_push = take((size_t)2 * item_cap * sizeof(uint2));
   const size_t o_counts = take((size_t)s.chunk * nseg * 4);
   const size_t o_raster = take((size_t)std::max<uint32_t>(s.raster_cap, 1) * 4);
   const size_t o_roff = take((size_t)(s.chunk + 1) * 4);
@@ -447,7 +449,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.state = (float4*)(mb + o_state);
   a.ring = (int*)(mb + o_ring);
   a.hist = (uint32_t*)(mb + o_hist);
-  a.active = (uint32_t*)(mb + o_active);
+  a.items = (uint2*)(mb + o_items_push);
+  a.item_cap = (uint32_t)item_cap;
   a.counts = (uint32_t*)(mb + o_counts);
   a.raster = (uint32_t*)(mb + o_raster);
   a.raster_off = (uint32_t*)(mb + o_roff);
@@ -766,9 +769,9 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
   const StepArgs& a = s.args;
   const double W = s.bf16 ? 2.0 : 4.0;
   // Algorithmic bytes: update = state 16 B read + 16 B write + ring 8 B per
-  // LIF cell, mask 4 B per input cell, 4 B per bitmap word; deliver = per
-  // walked push synapse 4 B word + W weight + 8 B atomic, per spike 4 B list +
-  // 8 B row offsets, per dense ELL entry 4 + W B plus 8 B per post.
+  // LIF cell, mask 4 B per input cell, 4 B per bitmap word, 8 B per push item
+  // written; deliver = per walked push synapse 4 B word + W weight + 8 B
+  // atomic, 8 B per push item read, per dense ELL entry 4 + W B plus 8 B per post.
   double upd_bytes = (double)a.n_words * 4.0;
   for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 40.0 * d.count : 4.0 * d.count;
   double pull_bytes = 0;
@@ -795,10 +798,10 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
       SGB_CUDA(cudaEventRecord(ev[3], s.stream));
       SGB_CUDA(cudaMemcpyAsync(&after, a.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s.stream));
       SGB_CUDA(cudaStreamSynchronize(s.stream));
-      const double spikes = (double)after.active_count[before.step & 1];
+      const double items = (double)after.active_count[before.step & 1];
       const double walked = (double)(after.delivered - before.delivered);
-      const double step_bytes[K] = {upd_bytes + spikes * 4.0,
-                                    walked * (12.0 + W) + spikes * 12.0 + pull_bytes};
+      const double step_bytes[K] = {upd_bytes + items * 8.0,
+                                    walked * (12.0 + W) + items * 8.0 + pull_bytes};
       for (int k = 0; k < K; ++k) {
         float ms = 0.f;
         SGB_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));

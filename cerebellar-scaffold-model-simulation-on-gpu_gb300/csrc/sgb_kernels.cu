@@ -151,16 +151,35 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
   const uint32_t n = __popc(ballot);
   const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
   const uint32_t ev = __reduce_add_sync(kFull, fired ? __ldg(a.outdeg + i) : 0u);
+  // Push work: the cell's push-table row cut into kPushChunk ranges, laid out
+  // by a warp-inclusive scan so one atomic reserves the warp's items.
+  uint32_t r0 = 0, r1 = 0, nit = 0;
+  if (fired && a.any_push) {
+    r0 = __ldg(a.push_row + i);
+    r1 = __ldg(a.push_row + i + 1);
+    nit = (r1 - r0 + kPushChunk - 1) / kPushChunk;
+  }
+  uint32_t incl = nit;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= (uint32_t)o) incl += v;
+  }
+  const uint32_t tot_items = __shfl_sync(kFull, incl, 31);
   uint32_t off = 0, roff = 0;
   Ctl* ctl = a.ctl;
   if (lane == 0) {
-    off = atomicAdd(&ctl->active_count[ix.t & 1], n);
+    if (tot_items) off = atomicAdd(&ctl->active_count[ix.t & 1], tot_items);
     atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], n);
     if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
     if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
   }
-  off = __shfl_sync(kFull, off, 0);
-  if (fired) __stcg(a.active + (size_t)(ix.t & 1) * a.n_pad + off + rank, i);
+  off = __shfl_sync(kFull, off, 0) + incl - nit;
+  uint2* items = a.items + (size_t)(ix.t & 1) * a.item_cap;
+  for (uint32_t k = 0; k < nit; ++k) {
+    const uint32_t q0 = r0 + k * kPushChunk;
+    __stcg(items + off + k, make_uint2(q0, min(q0 + kPushChunk, r1)));
+  }
   if (a.raster_cap) {
     roff = __shfl_sync(kFull, roff, 0);
     if (fired) {
@@ -173,20 +192,30 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
 }
 
 // ---- phase 2: deliveries ------------------------------------------------------
-// One warp walks the push-table row of spiking cell j (coalesced 128-byte
-// lines); returns the row length (lane 0 accounts it).
+// One warp delivers one push item (at most kPushChunk synapses of a spiking
+// cell's row): all loads of the item are issued before its atomics so the
+// item costs one memory round trip; returns the item's synapse count.
 template <bool BF16>
-__device__ __forceinline__ uint32_t push_spike(const StepArgs& a, uint32_t j, uint32_t slot0) {
+__device__ __forceinline__ uint32_t push_item(const StepArgs& a, uint2 it, uint32_t slot0) {
+  constexpr int kPer = kPushChunk / 32;
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t r0 = __ldg(a.push_row + j), r1 = __ldg(a.push_row + j + 1);
-  for (uint32_t q = r0 + lane; q < r1; q += 32) {
-    const uint32_t wd = __ldg(a.push_syn + q);
-    const int fx = __float2int_rn(load_weight<BF16>(a.push_w, q));
-    uint32_t slot = slot0 + ((wd >> kPushPostBits) & 15u);
-    if (slot >= a.ring_slots) slot -= a.ring_slots;
-    atomicAdd(a.ring + (((size_t)slot * a.n_pad + (wd & kPushPostMask)) << 1) + (wd >> 31), fx);
+  uint32_t wd[kPer];
+  float wv[kPer];
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const uint32_t q = it.x + k * 32 + lane;
+    wd[k] = q < it.y ? __ldg(a.push_syn + q) : 0u;
+    wv[k] = q < it.y ? load_weight<BF16>(a.push_w, q) : 0.f;
   }
-  return r1 - r0;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    if (it.x + k * 32 + lane >= it.y) break;
+    uint32_t slot = slot0 + ((wd[k] >> kPushPostBits) & 15u);
+    if (slot >= a.ring_slots) slot -= a.ring_slots;
+    atomicAdd(a.ring + (((size_t)slot * a.n_pad + (wd[k] & kPushPostMask)) << 1) + (wd[k] >> 31),
+              __float2int_rn(wv[k]));
+  }
+  return it.y - it.x;
 }
 
 __device__ __forceinline__ uint32_t spike_bit(const StepArgs& a, uint32_t hrow,
@@ -245,8 +274,8 @@ __device__ __forceinline__ void pull_item(const StepArgs& a, const PullItem& it,
 // Warp-level dispatch of delivery unit u: spikes first, then ELL tiles and items.
 template <bool BF16>
 __device__ __forceinline__ uint32_t deliver_unit(const StepArgs& a, uint32_t u, uint32_t n_act,
-                                                 const uint32_t* list, const StepIdx& ix) {
-  if (u < n_act) return push_spike<BF16>(a, __ldcg(list + u), ix.slot);
+                                                 const uint2* list, const StepIdx& ix) {
+  if (u < n_act) return push_item<BF16>(a, __ldcg(list + u), ix.slot);
   u -= n_act;
   if (u < a.n_pull_tiles) {
     pull_tile<BF16>(a, a.pull_tiles[u], ix);
@@ -286,7 +315,7 @@ __global__ void __launch_bounds__(kBlock) k_deliver(StepArgs a) {
   Ctl* ctl = a.ctl;
   const StepIdx ix = step_of(ctl);
   const uint32_t n_act = a.any_push ? ctl->active_count[ix.t & 1] : 0u;
-  const uint32_t* list = a.active + (size_t)(ix.t & 1) * a.n_pad;
+  const uint2* list = a.items + (size_t)(ix.t & 1) * a.item_cap;
   const uint32_t n_units = n_act + a.n_pull_tiles + a.n_pull_items;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t nw = (gridDim.x * kBlock) >> 5;
@@ -368,13 +397,13 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
 }
 
 template <bool BF16>
-__global__ void __launch_bounds__(kBlock) k_persistent(StepArgs a, uint32_t n_steps) {
+__global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(ctl);
   const unsigned long long t0 = ix.t;
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5;
-  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kPersistBlock) >> 5;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
   unsigned long long target = 0;
   uint32_t walked = 0;
@@ -387,7 +416,7 @@ __global__ void __launch_bounds__(kBlock) k_persistent(StepArgs a, uint32_t n_st
     if (!grid_barrier(a, target)) return;
     if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     const uint32_t n_act = a.any_push ? __ldcg(&ctl->active_count[ix.t & 1]) : 0u;
-    const uint32_t* list = a.active + (size_t)(ix.t & 1) * a.n_pad;
+    const uint2* list = a.items + (size_t)(ix.t & 1) * a.item_cap;
     const uint32_t n_units = n_act + a.n_pull_tiles + a.n_pull_items;
     for (uint32_t u = gw; u < n_units; u += nw) walked += deliver_unit<BF16>(a, u, n_act, list, ix);
     if (!grid_barrier(a, target)) return;
@@ -433,9 +462,9 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
 int persistent_blocks_per_sm(bool bf16) {
   int n = 0;
   if (bf16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true>, kPersistBlock, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, kPersistBlock, 0);
   return n;
 }
 
@@ -444,7 +473,7 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
   uint32_t n = n_steps;
   void* params[] = {&args, &n};
   const void* fn = a.bf16 ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
-  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kBlock), params, 0, s);
+  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, 0, s);
 }
 
 }  // namespace sgb

@@ -1,0 +1,124 @@
+// Standalone delivery operator on caller-owned device buffers.
+//
+// The reference exposes its propagation as free-standing kernels called once
+// per projection and step (spike_propagation, spike_propagation_mThreads,
+// spike_propagation_PR; Simulation_header.cu:83-303).  sgb_deliver_spikes is
+// the same operation for callers that run their own neuron update: given one
+// step's spike flags it adds every synapse of every spiking cell into the
+// fixed-point delay ring, event-driven.  Two kernels: a ballot compaction of
+// the spike flags into an active list (scratch), then one warp per active
+// cell walking its push-table row with coalesced loads and integer atomics.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/scaffold_gb300.h"
+#include "sgb_device.h"
+#include "sgb_model.h"
+
+namespace sgb {
+namespace {
+
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// Scratch layout: [0] active count, [64..] active cell ids (256-byte aligned).
+constexpr uint32_t kListOffset = 64;
+
+__global__ void __launch_bounds__(kBlock) k_ops_compact(const uint8_t* __restrict__ spikes,
+                                                        uint32_t n, uint32_t* scratch) {
+  const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+  const bool f = i < n && spikes[i] != 0;
+  const uint32_t ballot = __ballot_sync(kFullMask, f);
+  if (!ballot) return;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t off = 0;
+  if (lane == 0) off = atomicAdd(scratch, (uint32_t)__popc(ballot));
+  off = __shfl_sync(kFullMask, off, 0);
+  if (f) scratch[kListOffset + off + __popc(ballot & ((1u << lane) - 1u))] = i;
+}
+
+template <bool BF16>
+__global__ void __launch_bounds__(kBlock) k_ops_push(const uint32_t* scratch,
+                                                     const uint32_t* __restrict__ row,
+                                                     const uint32_t* __restrict__ syn,
+                                                     const void* __restrict__ w, int* ring,
+                                                     uint32_t n, uint32_t slots, uint32_t slot0) {
+  const uint32_t n_act = scratch[0];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nw = (gridDim.x * kBlock) >> 5;
+  for (uint32_t e = (blockIdx.x * kBlock + threadIdx.x) >> 5; e < n_act; e += nw) {
+    const uint32_t j = scratch[kListOffset + e];
+    const uint32_t r0 = __ldg(row + j), r1 = __ldg(row + j + 1);
+    for (uint32_t q = r0 + lane; q < r1; q += 32) {
+      const uint32_t wd = __ldg(syn + q);
+      const float wf = BF16 ? __uint_as_float(((uint32_t)__ldg((const unsigned short*)w + q)) << 16)
+                            : __ldg((const float*)w + q);
+      uint32_t slot = slot0 + ((wd >> kPushPostBits) & 15u);
+      if (slot >= slots) slot -= slots;
+      atomicAdd(ring + (((size_t)slot * n + (wd & kPushPostMask)) << 1) + (wd >> 31),
+                __float2int_rn(wf));
+    }
+  }
+}
+
+}  // namespace
+
+int deliver_check(int32_t n_cells, int32_t weight_type, int32_t ring_slots, int64_t step,
+                  const void* spikes, const void* row, const void* syn, const void* w,
+                  const void* ring) {
+  if (n_cells < 0 || (uint32_t)n_cells > kPushPostMask)
+    return set_error(SGB_ERR_ARG, "n_cells %d not in 0..2^27-1", n_cells);
+  if (weight_type != SGB_WEIGHT_FP32 && weight_type != SGB_WEIGHT_BF16)
+    return set_error(SGB_ERR_ARG, "unknown weight type %d", weight_type);
+  if (ring_slots < 2 || ring_slots > kMaxDelay + 1)
+    return set_error(SGB_ERR_ARG, "ring_slots %d not in 2..%d", ring_slots, kMaxDelay + 1);
+  if (step < 0) return set_error(SGB_ERR_ARG, "step is negative");
+  if (n_cells && (!spikes || !row || !syn || !w || !ring))
+    return set_error(SGB_ERR_ARG, "NULL device buffer");
+  return SGB_OK;
+}
+
+// Compaction + push on `scratch` (count word + list of n_cells ids).
+cudaError_t deliver_enqueue(const uint8_t* spikes, int32_t n_cells, const uint32_t* row,
+                            const uint32_t* syn, const void* w, int32_t weight_type, int32_t* ring,
+                            int32_t ring_slots, int64_t step, uint32_t* scratch,
+                            cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), st);
+  if (e || !n_cells) return e;
+  const uint32_t n = (uint32_t)n_cells;
+  k_ops_compact<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(spikes, n, scratch);
+  if ((e = cudaGetLastError())) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint32_t slot0 = (uint32_t)(step % ring_slots);
+  const int blocks = 2 * (sms > 0 ? sms : 1);
+  if (weight_type == SGB_WEIGHT_BF16)
+    k_ops_push<true><<<blocks, kBlock, 0, st>>>(scratch, row, syn, w, ring, n,
+                                                 (uint32_t)ring_slots, slot0);
+  else
+    k_ops_push<false><<<blocks, kBlock, 0, st>>>(scratch, row, syn, w, ring, n,
+                                                  (uint32_t)ring_slots, slot0);
+  return cudaGetLastError();
+}
+
+}  // namespace sgb
+
+using namespace sgb;
+
+extern "C" int sgb_deliver_spikes(const uint8_t* spikes, int32_t n_cells, const uint32_t* row,
+                                  const uint32_t* syn, const void* weights, int32_t weight_type,
+                                  int32_t* ring, int32_t ring_slots, int64_t step, void* stream) {
+  int rc = deliver_check(n_cells, weight_type, ring_slots, step, spikes, row, syn, weights, ring);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint32_t* scratch = nullptr;
+  const size_t bytes = ((size_t)kListOffset + (size_t)n_cells) * sizeof(uint32_t);
+  cudaError_t e = cudaMallocAsync((void**)&scratch, bytes, st);
+  if (e) return set_error(SGB_ERR_CUDA, "cudaMallocAsync of %zu scratch bytes: %s", bytes, cudaGetErrorString(e));
+  e = deliver_enqueue(spikes, n_cells, row, syn, weights, weight_type, ring, ring_slots, step,
+                      scratch, st);
+  cudaError_t e2 = cudaFreeAsync(scratch, st);
+  if (e) return set_error(SGB_ERR_CUDA, "delivery launch failed: %s", cudaGetErrorString(e));
+  if (e2) return set_error(SGB_ERR_CUDA, "cudaFreeAsync: %s", cudaGetErrorString(e2));
+  return SGB_OK;
+}

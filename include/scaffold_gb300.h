@@ -290,6 +290,22 @@ int sgb_sim_launch_count(const sgb_sim* sim, int64_t* launches);
 int sgb_sim_profile(sgb_sim* sim, int32_t n_steps, double* mean_us, double* bytes_per_launch,
                     int64_t* launches);
 
+/* ---- standalone operator (caller-owned device buffers) -------------------- */
+/* Replaces the reference's per-projection propagation kernels spike_propagation,
+ * spike_propagation_mThreads and spike_propagation_PR (Simulation_header.cu:
+ * 83-303) as one operator for callers that run their own neuron update.  For
+ * every cell j with spikes[j] != 0 and every synapse q in [row[j], row[j+1]):
+ *   post = syn[q] & (2^27 - 1), d = (syn[q] >> 27) & 15, a = syn[q] >> 31,
+ *   ring[((step + d) % ring_slots) * n_cells + post][a] += rint(weights[q]),
+ * where weights are FP32 or BF16 already multiplied by the accumulator's 2^S.
+ * All pointers are device pointers; work is enqueued on `stream` (a
+ * cudaStream_t as void*, NULL = legacy default stream) and the call returns
+ * without waiting.  Scratch for the active-cell list is taken from the
+ * stream-ordered pool (cudaMallocAsync) and released on the same stream. */
+int sgb_deliver_spikes(const uint8_t* spikes, int32_t n_cells, const uint32_t* row,
+                       const uint32_t* syn, const void* weights, int32_t weight_type,
+                       int32_t* ring, int32_t ring_slots, int64_t step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

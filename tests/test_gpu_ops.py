@@ -1,0 +1,90 @@
+"""Standalone delivery operator (sgb_deliver_spikes) on caller-owned device buffers.
+
+Checked against a numpy restatement of the operation: for each spiking cell,
+every synapse of its push-table row adds rint(weight) to ring slot
+(step + delay) % slots of its target's accumulator.  Integer sums: exact.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_py
+import scaffold_gb300 as sg
+from scaffold_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_bits(x: np.ndarray) -> np.ndarray:
+    u = x.astype(np.float32).view(np.uint32).astype(np.uint64)
+    return ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def push_table(net, bf16: bool):
+    """Cell-major push table over every projection of `net` (unpadded ids)."""
+    d = oracle_py.describe(net)
+    o = oracle_py.Oracle(d, seed=1, bf16=bf16)
+    base = np.cumsum([0] + [p["num"] for p in d["pops"]])
+    n = int(base[-1])
+    pre_g, word, wsc = [], [], []
+    for pr in d["projs"]:
+        s = o.scale_bits(pr["post"], pr["channel"])
+        w = pr["weight"].astype(np.float32)
+        if bf16:
+            w = (bf16_bits(w).astype(np.uint32) << 16).view(np.float32)
+        ws = (w * np.float32(2.0 ** s)).astype(np.float32)
+        pre_g.append(base[pr["pre"]] + pr["pre_idx"].astype(np.int64))
+        word.append((base[pr["post"]] + pr["post_idx"].astype(np.uint64))
+                    | (pr["delay"].astype(np.uint64) << 27) | (np.uint64(pr["channel"]) << 31))
+        wsc.append(ws)
+    pre_g, word, wsc = np.concatenate(pre_g), np.concatenate(word), np.concatenate(wsc)
+    order = np.argsort(pre_g, kind="stable")
+    row = np.zeros(n + 1, np.int64)
+    np.add.at(row, pre_g + 1, 1)
+    row = np.cumsum(row).astype(np.uint32)
+    return n, row, word[order].astype(np.uint32), wsc[order]
+
+
+def expected(ring, n, row, syn, wsc, spikes, step, slots):
+    for j in np.flatnonzero(spikes):
+        for q in range(row[j], row[j + 1]):
+            post, dl, ch = syn[q] & ((1 << 27) - 1), (syn[q] >> 27) & 15, syn[q] >> 31
+            ring[(step + dl) % slots, post, ch] += int(np.rint(wsc[q]))
+
+
+@pytest.mark.parametrize("bf16", [False, True])
+def test_deliver_spikes_matches_restatement(bf16):
+    import torch
+
+    net = sg.scaffold(1, 0.25, 17)
+    n, row, syn, wsc = push_table(net, bf16)
+    slots = 5
+    dev = torch.device("cuda")
+    t_row = torch.from_numpy(row.view(np.int32)).to(dev)
+    t_syn = torch.from_numpy(syn.view(np.int32)).to(dev)
+    if bf16:
+        t_w = torch.from_numpy(bf16_bits(wsc).view(np.int16)).to(dev)
+    else:
+        t_w = torch.from_numpy(wsc).to(dev)
+    ring = torch.zeros((slots, n, 2), dtype=torch.int32, device=dev)
+    exp = np.zeros((slots, n, 2), np.int64)
+    rng = np.random.default_rng(5)
+    stream = torch.cuda.current_stream().cuda_stream
+    for step in (0, 3, 7):
+        spikes = (rng.random(n) < 0.08).astype(np.uint8)
+        t_sp = torch.from_numpy(spikes).to(dev)
+        rc = L.lib().sgb_deliver_spikes(t_sp.data_ptr(), n, t_row.data_ptr(), t_syn.data_ptr(),
+                                        t_w.data_ptr(), 1 if bf16 else 0, ring.data_ptr(),
+                                        slots, step, stream)
+        L.check(rc)
+        expected(exp, n, row, syn, wsc, spikes, step, slots)
+    torch.cuda.synchronize()
+    assert np.array_equal(ring.cpu().numpy().astype(np.int64), exp)
+    assert exp.any()
+
+
+def test_deliver_spikes_argument_errors():
+    assert L.lib().sgb_deliver_spikes(None, 10, None, None, None, 0, None, 5, 0, None) == -1
+    assert L.lib().sgb_deliver_spikes(None, 0, None, None, None, 0, None, 1, 0, None) == -1
+    assert L.lib().sgb_deliver_spikes(None, 0, None, None, None, 0, None, 5, 0, None) == 0
