@@ -13,7 +13,7 @@ import oracle_py
 import scaffold_gb300 as sg
 from scaffold_gb300 import _lib as L
 
-pytestmark = pytest.mark.gpu
+gpu = pytest.mark.gpu
 
 
 def bf16_bits(x: np.ndarray) -> np.ndarray:
@@ -34,9 +34,10 @@ def push_table(net, bf16: bool):
         if bf16:
             w = (bf16_bits(w).astype(np.uint32) << 16).view(np.float32)
         ws = (w * np.float32(2.0 ** s)).astype(np.float32)
-        pre_g.append(base[pr["pre"]] + pr["pre_idx"].astype(np.int64))
-        word.append((base[pr["post"]] + pr["post_idx"].astype(np.uint64))
-                    | (pr["delay"].astype(np.uint64) << 27) | (np.uint64(pr["channel"]) << 31))
+        pre_g.append(np.int64(base[pr["pre"]]) + pr["pre_idx"].astype(np.int64))
+        post_g = np.uint64(base[pr["post"]]) + pr["post_idx"].astype(np.uint64)
+        word.append(post_g | (pr["delay"].astype(np.uint64) << np.uint64(27))
+                    | (np.uint64(pr["channel"]) << np.uint64(31)))
         wsc.append(ws)
     pre_g, word, wsc = np.concatenate(pre_g), np.concatenate(word), np.concatenate(wsc)
     order = np.argsort(pre_g, kind="stable")
@@ -48,11 +49,23 @@ def push_table(net, bf16: bool):
 
 def expected(ring, n, row, syn, wsc, spikes, step, slots):
     for j in np.flatnonzero(spikes):
-        for q in range(row[j], row[j + 1]):
-            post, dl, ch = syn[q] & ((1 << 27) - 1), (syn[q] >> 27) & 15, syn[q] >> 31
+        for q in range(int(row[j]), int(row[j + 1])):
+            s = int(syn[q])
+            post, dl, ch = s & ((1 << 27) - 1), (s >> 27) & 15, s >> 31
             ring[(step + dl) % slots, post, ch] += int(np.rint(wsc[q]))
 
 
+def test_push_table_helper_cpu():
+    """The restatement used by the GPU checks covers every synapse once (no GPU)."""
+    net = sg.scaffold(1, 0.25, 17)
+    n, row, syn, wsc = push_table(net, False)
+    assert row[-1] == net.counts()["synapses"] == len(syn) == len(wsc)
+    ring = np.zeros((5, n, 2), np.int64)
+    expected(ring, n, row, syn, wsc, np.ones(n, np.uint8), 0, 5)
+    assert ring[0].sum() == 0 and ring[1:].sum() > 0
+
+
+@gpu
 @pytest.mark.parametrize("bf16", [False, True])
 def test_deliver_spikes_matches_restatement(bf16):
     import torch
@@ -84,6 +97,7 @@ def test_deliver_spikes_matches_restatement(bf16):
     assert exp.any()
 
 
+@gpu
 def test_deliver_spikes_argument_errors():
     assert L.lib().sgb_deliver_spikes(None, 10, None, None, None, 0, None, 5, 0, None) == -1
     assert L.lib().sgb_deliver_spikes(None, 0, None, None, None, 0, None, 1, 0, None) == -1
