@@ -59,6 +59,25 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def aggregate(pg, device, ms: float, events: float):
+    """Whole-job numbers of one timed region: max wall time over ranks (the job
+    finishes with its slowest replica) and the sum of events over ranks."""
+    import torch
+
+    if pg is None:
+        return ms, events
+    tm = torch.tensor([ms], dtype=torch.float64, device=device)
+    te = torch.tensor([events], dtype=torch.float64, device=device)
+    pg.all_reduce(tm, op=pg.ReduceOp.MAX)
+    pg.all_reduce(te, op=pg.ReduceOp.SUM)
+    return float(tm[0]), float(te[0])
+
+
+def realtime_factor(world: int, bench_steps: int, bio_s_per_step: float, ms: float) -> float:
+    """Biological seconds simulated by all replicas per wall second."""
+    return world * bench_steps * bio_s_per_step / (ms / 1000.0)
+
+
 def build_nets(wl: dict, rank: int):
     import scaffold_gb300 as sg
 
@@ -247,15 +266,8 @@ def run_gb300(a):
     ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
     events = sim.info().events - ev0
     launches = sim.launch_count() - l0
-    t = torch.tensor([ms, float(events)], dtype=torch.float64, device="cuda")
-    if pg:
-        tm = t.clone()
-        pg.all_reduce(tm, op=pg.ReduceOp.MAX)
-        pg.all_reduce(t, op=pg.ReduceOp.SUM)
-        ms_max, events_all = float(tm[0]), float(t[1])
-    else:
-        ms_max, events_all = ms, float(events)
-    value = world * a.steps * bio_per_step / (ms_max / 1000.0)
+    ms_max, events_all = aggregate(pg, "cuda", ms, float(events))
+    value = realtime_factor(world, a.steps, bio_per_step, ms_max)
 
     # End to end through the C ABI: new input rates from host memory before
     # each step, per-step spike counts of every population back to the host.
@@ -271,12 +283,9 @@ def run_gb300(a):
         for k in range(len(nets)):
             sim.set_input_freq(k, rates)
         counts, _ = sim.loop_n_steps(a.chunk, counts=True)
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        pg.all_reduce(te, op=pg.ReduceOp.MAX)
-        e2e_s = float(te[0])
-    e2e = {"value": world * e2e_steps * bio_per_step / e2e_s, "unit": "x realtime",
+    e2e_s, _ = aggregate(pg, "cuda", time.perf_counter() - t0, 0.0)
+    e2e = {"value": realtime_factor(world, e2e_steps, bio_per_step, e2e_s * 1000.0),
+           "unit": "x realtime",
            "h2d_bytes_per_step": 56 * n_src * len(nets),
            "d2h_bytes_per_step": 4 * a.chunk * info.n_segments + 4}
 

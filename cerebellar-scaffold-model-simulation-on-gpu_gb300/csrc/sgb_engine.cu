@@ -755,9 +755,174 @@ int sim_set_stream(Sim& s, cudaStream_t st) {
   return SGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner.  Decisions: propagation mode per projection group (projection j
+// of every instance; instances of one handle share an architecture or are
+// tuned per net when they do not) and the step driver (persistent vs graph).
+// Each candidate runs n_steps of the live simulation, timed with CUDA events
+// on the handle's stream, from the same snapshot of the device state; the
+// snapshot is restored at the end, so tuning does not advance the simulation.
+
+static uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+  return h;
+}
+
+static std::string tune_signature(const Sim& s) {
+  uint64_t h = 1469598103934665603ull;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, s.cfg.device) == cudaSuccess)
+    h = fnv1a(h, prop.name, strlen(prop.name));
+  const int32_t hdr[4] = {(int32_t)s.nets.size(), s.cfg.substeps, s.cfg.weight_type, (int32_t)s.chunk};
+  h = fnv1a(h, hdr, sizeof hdr);
+  h = fnv1a(h, &s.cfg.dt_ms, sizeof s.cfg.dt_ms);
+  for (const Network& net : s.nets) {
+    for (const Population& p : net.pops) h = fnv1a(h, &p.num, sizeof p.num);
+    for (const Projection& pr : net.projs) {
+      const int64_t v[4] = {pr.pre, pr.post, pr.channel, (int64_t)pr.pre_idx.size()};
+      h = fnv1a(h, v, sizeof v);
+    }
+  }
+  char buf[32];
+  snprintf(buf, sizeof buf, "%016llx", (unsigned long long)h);
+  return buf;
+}
+
+// Reads the cached decision for `sig` from a JSON-lines file:
+// {"signature": "<hex>", "exec_mode": m, "modes": [a, b, ...], "us_per_step": x}
+static bool tune_cache_read(const char* path, const std::string& sig, int32_t* exec_mode,
+                            std::vector<int32_t>& modes) {
+  FILE* f = path ? fopen(path, "rb") : nullptr;
+  if (!f) return false;
+  char line[1 << 16];
+  bool found = false;
+  while (!found && fgets(line, sizeof line, f)) {
+    if (!strstr(line, ("\"signature\": \"" + sig + "\"").c_str())) continue;
+    const char* e = strstr(line, "\"exec_mode\":");
+    const char* m = strstr(line, "\"modes\": [");
+    if (!e || !m) continue;
+    *exec_mode = atoi(e + 12);
+    modes.clear();
+    for (const char* p = m + 10; *p && *p != ']';) {
+      char* q;
+      const long v = strtol(p, &q, 10);
+      if (q == p) { ++p; continue; }
+      modes.push_back((int32_t)v);
+      p = q;
+    }
+    found = true;
+  }
+  fclose(f);
+  return found;
+}
+
+static void tune_cache_write(const char* path, const std::string& sig, int32_t exec_mode,
+                             const std::vector<int32_t>& modes, double us_per_step) {
+  if (!path) return;
+  FILE* f = fopen(path, "ab");
+  if (!f) return;
+  fprintf(f, "{\"signature\": \"%s\", \"exec_mode\": %d, \"modes\": [", sig.c_str(), exec_mode);
+  for (size_t i = 0; i < modes.size(); ++i) fprintf(f, "%s%d", i ? ", " : "", modes[i]);
+  fprintf(f, "], \"us_per_step\": %.4f}\n", us_per_step);
+  fclose(f);
+}
+
+static int apply_modes(Sim& s, const std::vector<int32_t>& modes) {
+  if (modes.size() != s.projs.size()) return set_error(SGB_ERR_ARG, "mode vector length mismatch");
+  for (size_t k = 0; k < modes.size(); ++k) s.projs[k].mode = (uint32_t)modes[k];
+  return upload_modes(s);
+}
+
 int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
-  (void)s; (void)n_steps; (void)cache_path;
-  return set_error(SGB_ERR_UNSUPPORTED, "autotuner not available in this build");
+  if (n_steps < 1) return set_error(SGB_ERR_ARG, "n_steps must be >= 1");
+  const std::string sig = tune_signature(s);
+  std::vector<int32_t> modes;
+  int32_t exec_mode = s.cfg.exec_mode;
+  if (tune_cache_read(cache_path, sig, &exec_mode, modes) && modes.size() == s.projs.size()) {
+    s.cfg.exec_mode = exec_mode;
+    return apply_modes(s, modes);
+  }
+  // Snapshot of the device state a run changes.
+  const StepArgs& a = s.args;
+  const size_t b_state = (size_t)s.n_pad * sizeof(float4);
+  const size_t b_ring = (size_t)s.ring_slots * s.n_pad * 8;
+  const size_t b_hist = (size_t)s.hist_rows * s.n_words * 4;
+  const size_t b_tot = s.segs.size() * sizeof(double);
+  const size_t total = b_state + b_ring + b_hist + sizeof(Ctl) + b_tot;
+  char* snap = nullptr;
+  SGB_CUDA(cudaMalloc(&snap, total));
+  auto save = [&](bool restore) -> cudaError_t {
+    struct { void* dev; size_t n; } parts[5] = {{a.state, b_state}, {a.ring, b_ring}, {a.hist, b_hist},
+                                              {a.ctl, sizeof(Ctl)}, {a.totals, b_tot}};
+    size_t o = 0;
+    for (auto& p : parts) {
+      cudaError_t e = restore ? cudaMemcpyAsync(p.dev, snap + o, p.n, cudaMemcpyDeviceToDevice, s.stream)
+                              : cudaMemcpyAsync(snap + o, p.dev, p.n, cudaMemcpyDeviceToDevice, s.stream);
+      if (e) return e;
+      o += p.n;
+    }
+    return cudaStreamSynchronize(s.stream);
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = SGB_OK;
+  auto fail = [&](int code) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(snap);
+    return code;
+  };
+  if (save(false) || cudaEventCreate(&e0) || cudaEventCreate(&e1))
+    return fail(set_error(SGB_ERR_CUDA, "autotune snapshot failed"));
+  // One candidate: restore, warm up, time n_steps.
+  auto measure = [&](double* us) -> int {
+    if (save(true)) return set_error(SGB_ERR_CUDA, "autotune restore failed");
+    int r = sim_enqueue(s, std::max(1, n_steps / 4));
+    if (r) return r;
+    cudaEventRecord(e0, s.stream);
+    r = sim_enqueue(s, n_steps);
+    if (r) return r;
+    cudaEventRecord(e1, s.stream);
+    r = sim_sync(s);
+    if (r) return r;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e0, e1)) return set_error(SGB_ERR_CUDA, "autotune timing failed");
+    *us = 1000.0 * ms / n_steps;
+    return SGB_OK;
+  };
+  // Projection groups: the j-th projection of every net with j projections.
+  size_t max_proj = 0;
+  for (const Network& net : s.nets) max_proj = std::max(max_proj, net.projs.size());
+  modes.assign(s.projs.size(), SGB_PROP_CSR);
+  for (size_t k = 0; k < s.projs.size(); ++k)
+    if (!s.projs[k].ell_K) modes[k] = SGB_PROP_CSR;
+  double best = 0;
+  if ((rc = apply_modes(s, modes)) || (rc = measure(&best))) return fail(rc);
+  for (size_t j = 0; j < max_proj; ++j) {
+    std::vector<int32_t> trial = modes;
+    bool any = false;
+    for (size_t k = 0; k < s.ptab.size(); ++k)
+      if ((size_t)s.ptab[k].proj == j && s.projs[k].ell_K) { trial[k] = SGB_PROP_ELL; any = true; }
+    if (!any) continue;
+    double us = 0;
+    if ((rc = apply_modes(s, trial)) || (rc = measure(&us))) return fail(rc);
+    if (us < best * 0.98) { best = us; modes = trial; }
+  }
+  if ((rc = apply_modes(s, modes))) return fail(rc);
+  // Step driver.
+  const int32_t other = s.cfg.exec_mode == SGB_EXEC_PERSISTENT ? SGB_EXEC_GRAPH : SGB_EXEC_PERSISTENT;
+  const int32_t mine = s.cfg.exec_mode;
+  s.cfg.exec_mode = other;
+  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
+  s.graphs.clear();
+  double us_other = 0;
+  if ((rc = measure(&us_other))) return fail(rc);
+  if (us_other < best * 0.98) best = us_other; else s.cfg.exec_mode = mine;
+  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
+  s.graphs.clear();
+  if (save(true)) return fail(set_error(SGB_ERR_CUDA, "autotune restore failed"));
+  tune_cache_write(cache_path, sig, s.cfg.exec_mode, modes, best);
+  return fail(SGB_OK);
 }
 
 // Instrumented run: the per-step kernels launched one by one, each bracketed

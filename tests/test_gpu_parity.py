@@ -177,3 +177,28 @@ def test_determinism_two_runs():
     ua, ga, _ = a.state()
     ub, gb, _ = b.state()
     assert np.array_equal(ga.view(np.uint32), gb.view(np.uint32))
+
+
+def test_autotune_keeps_state_and_caches(tmp_path):
+    """The autotuner times candidates from a snapshot and restores it: after
+    tuning, the simulation continues exactly as the oracle does."""
+    net = sg.scaffold(1, 0.25, 19)
+    sim = sg.Simulation([net], [19], chunk_steps=250)
+    o = oracle_py.Oracle(oracle_py.describe(net), seed=19)
+    c0, _ = sim.loop_n_steps(300)
+    e0, _ = o.run(300)
+    assert np.array_equal(c0, e0)
+    cache = str(tmp_path / "tune.jsonl")
+    sim.autotune(200, cache)
+    assert sim.info().step == 300
+    modes = [sim.get_propagation(0, j) for j in range(len(net.projections))]
+    assert set(modes) <= {sg.PROP_CSR, sg.PROP_ELL}
+    c1, _ = sim.loop_n_steps(500)
+    e1, _ = o.run(500)
+    assert np.array_equal(c1, e1)
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 1 and '"signature"' in lines[0]
+    other = sg.Simulation([net], [19], chunk_steps=250)
+    other.autotune(200, cache)  # served from the cache: no new line
+    assert [other.get_propagation(0, j) for j in range(len(net.projections))] == modes
+    assert len(open(cache).read().splitlines()) == 1
