@@ -51,7 +51,8 @@ def test_bf16_and_fp32_against_fp64_oracle():
     for name, wt in (("fp32", sg.WEIGHT_FP32), ("bf16", sg.WEIGHT_BF16)):
         sim = sg.Simulation([net], [1], weight_type=wt, raster=True)
         c, (ids, offs) = sim.loop_n_steps(STEPS, raster=True, raster_cap=1 << 24)
-        rate_err = (c.sum(0) - c64.sum(0)) / np.maximum(c64.sum(0), 1)
+        tot, tot64 = c.sum(0).astype(np.int64), c64.sum(0).astype(np.int64)
+        rate_err = (tot - tot64) / np.maximum(tot64, 1)
         out[name] = {
             "first_divergence_step": _first_div(ids, offs, i64, o64),
             "matched_within_1_step": _match_within_one(ids, offs, i64, o64, net.counts()["neurons"]),
