@@ -13,7 +13,8 @@
 //   history    spike bitmaps of the last H = max delay steps (1 bit per cell).
 //   items      push work of the current step: for every spiking cell, its
 //              push-table row cut into ranges of at most kPushChunk synapses
-//              (uint2 {first, end}); double-buffered by step parity.
+//              (uint2 {first synapse, length << 23 | step tag}); a delivered
+//              item is cleared; double-buffered by step parity.
 //   push table one cell-major CSR over every projection in event-driven mode
 //              (all instances): synapse word = padded post index | delay << 27
 //              | accumulator << 31, plus the weight pre-multiplied by its
@@ -86,7 +87,7 @@ struct Ctl {
   uint32_t ring_slot;             // step % D
   uint32_t hist_row;              // step % H
   uint32_t t_rel;                 // step index within the current chunk
-  uint32_t active_count[2];       // push items of step s live in buffer s & 1
+  uint32_t active_count[2];       // push items reserved in buffer s & 1 at step s
   uint32_t raster_count;          // spikes recorded in the current chunk
   uint32_t error;                 // device error bits (kErr*)
   uint32_t barrier_gen;           // persistent-kernel grid barrier state

@@ -514,6 +514,7 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
   SGB_CUDA(cudaMemsetAsync(a.ring, 0, (size_t)s.ring_slots * s.n_pad * 8, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.hist, 0, (size_t)s.hist_rows * s.n_words * 4, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.items, 0, (size_t)2 * a.item_cap * sizeof(uint2), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.totals, 0, s.segs.size() * sizeof(double), s.stream));
   SGB_CUDA(cudaStreamSynchronize(s.stream));
   return SGB_OK;

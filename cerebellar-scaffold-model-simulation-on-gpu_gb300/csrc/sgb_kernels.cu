@@ -122,43 +122,43 @@ __device__ __forceinline__ bool lif_update(const SegDev& sd, int substeps, float
 }
 
 // ---- phase 1: one warp updates the 32 cells of word w --------------------------
-// Cross-block data (ring slots written by other SMs' atomics, counters) is read
-// with ld.global.cg so a persistent kernel never sees a stale L1 line.
-__device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
+// Cross-block data (ring slots written by other SMs' atomics, counters, push
+// items) is accessed with ld/st.global.cg so a persistent kernel never sees a
+// stale L1 line.
+
+// Push items carry the step that produced them; a consumer clears each item
+// it delivers, so the delivery phase finds the end of the list without
+// reading the item count.
+__device__ __forceinline__ uint32_t item_tag(unsigned long long t) {
+  return ((uint32_t)t & 0x3FFFFFu) | 0x400000u;  // never 0 (cleared)
+}
+
+// One cell's step; state and constants in registers, ring slot consumed.
+__device__ __forceinline__ bool cell_fire(const StepArgs& a, const SegDev& sd, uint32_t i,
+                                          uint32_t local, bool valid, float4& st, uint32_t mask,
+                                          const StepIdx& ix) {
+  if (!valid) return false;
+  if (sd.kind == kSegInput) return mask ? input_fire(a, sd, local, mask, ix.t) : false;
+  int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i;
+  const int2 acc = __ldcg(rp);
+  if (acc.x | acc.y) __stcg(rp, make_int2(0, 0));
+  return lif_update(sd, a.substeps, st, acc);
+}
+
+// Spike bookkeeping of one word: bitmap word, per-segment count, event count,
+// raster entries, and the spiking cells' push rows cut into kPushChunk items
+// laid out by a warp-inclusive scan (one atomic reserves the warp's items).
+__device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint32_t seg,
+                                             uint32_t i, bool fired, uint32_t r0, uint32_t r1,
+                                             uint32_t outdeg, const StepIdx& ix) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t seg = __ldg(a.seg_of_word + w);
-  const SegDev& sd = a.segs[seg];
-  const uint32_t i = (w << 5) + lane;
-  const uint32_t local = i - sd.base;
-  const bool valid = local < sd.count;
-  bool fired = false;
-  if (valid) {
-    if (sd.kind == kSegInput) {
-      const uint32_t mask = __ldg(a.src_mask + i);
-      if (mask) fired = input_fire(a, sd, local, mask, ix.t);
-    } else {
-      int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i;
-      const int2 acc = __ldcg(rp);
-      if (acc.x | acc.y) __stcg(rp, make_int2(0, 0));
-      float4 st = a.state[i];
-      fired = lif_update(sd, a.substeps, st, acc);
-      a.state[i] = st;
-    }
-  }
   const uint32_t ballot = __ballot_sync(kFull, fired);
   if (lane == 0) __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, ballot);
   if (ballot == 0) return;
   const uint32_t n = __popc(ballot);
   const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
-  const uint32_t ev = __reduce_add_sync(kFull, fired ? __ldg(a.outdeg + i) : 0u);
-  // Push work: the cell's push-table row cut into kPushChunk ranges, laid out
-  // by a warp-inclusive scan so one atomic reserves the warp's items.
-  uint32_t r0 = 0, r1 = 0, nit = 0;
-  if (fired && a.any_push) {
-    r0 = __ldg(a.push_row + i);
-    r1 = __ldg(a.push_row + i + 1);
-    nit = (r1 - r0 + kPushChunk - 1) / kPushChunk;
-  }
+  const uint32_t ev = __reduce_add_sync(kFull, fired ? outdeg : 0u);
+  const uint32_t nit = fired ? (r1 - r0 + kPushChunk - 1) / kPushChunk : 0u;
   uint32_t incl = nit;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -176,9 +176,11 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
   }
   off = __shfl_sync(kFull, off, 0) + incl - nit;
   uint2* items = a.items + (size_t)(ix.t & 1) * a.item_cap;
+  const uint32_t tag = item_tag(ix.t);
   for (uint32_t k = 0; k < nit; ++k) {
     const uint32_t q0 = r0 + k * kPushChunk;
-    __stcg(items + off + k, make_uint2(q0, min(q0 + kPushChunk, r1)));
+    const uint32_t len = min(kPushChunk, r1 - q0);
+    __stcg(items + off + k, make_uint2(q0, (len << 23) | tag));
   }
   if (a.raster_cap) {
     roff = __shfl_sync(kFull, roff, 0);
@@ -191,6 +193,29 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
   }
 }
 
+// General form: everything read from global memory.
+__device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t seg = __ldg(a.seg_of_word + w);
+  const SegDev& sd = a.segs[seg];
+  const uint32_t i = (w << 5) + lane;
+  const uint32_t local = i - sd.base;
+  const bool valid = local < sd.count;
+  uint32_t mask = 0, r0 = 0, r1 = 0, od = 0;
+  float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (valid) {
+    if (sd.kind == kSegInput) mask = __ldg(a.src_mask + i); else st = a.state[i];
+    od = __ldg(a.outdeg + i);
+    if (a.any_push) {
+      r0 = __ldg(a.push_row + i);
+      r1 = __ldg(a.push_row + i + 1);
+    }
+  }
+  const bool fired = cell_fire(a, sd, i, local, valid, st, mask, ix);
+  if (valid && sd.kind == kSegLif) a.state[i] = st;
+  publish_word(a, w, seg, i, fired, r0, r1, od, ix);
+}
+
 // ---- phase 2: deliveries ------------------------------------------------------
 // One warp delivers one push item (at most kPushChunk synapses of a spiking
 // cell's row): all loads of the item are issued before its atomics so the
@@ -199,23 +224,24 @@ template <bool BF16>
 __device__ __forceinline__ uint32_t push_item(const StepArgs& a, uint2 it, uint32_t slot0) {
   constexpr int kPer = kPushChunk / 32;
   const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t q1 = it.x + (it.y >> 23);
   uint32_t wd[kPer];
   float wv[kPer];
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
     const uint32_t q = it.x + k * 32 + lane;
-    wd[k] = q < it.y ? __ldg(a.push_syn + q) : 0u;
-    wv[k] = q < it.y ? load_weight<BF16>(a.push_w, q) : 0.f;
+    wd[k] = q < q1 ? __ldg(a.push_syn + q) : 0u;
+    wv[k] = q < q1 ? load_weight<BF16>(a.push_w, q) : 0.f;
   }
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
-    if (it.x + k * 32 + lane >= it.y) break;
+    if (it.x + k * 32 + lane >= q1) break;
     uint32_t slot = slot0 + ((wd[k] >> kPushPostBits) & 15u);
     if (slot >= a.ring_slots) slot -= a.ring_slots;
     atomicAdd(a.ring + (((size_t)slot * a.n_pad + (wd[k] & kPushPostMask)) << 1) + (wd[k] >> 31),
               __float2int_rn(wv[k]));
   }
-  return it.y - it.x;
+  return it.y >> 23;
 }
 
 __device__ __forceinline__ uint32_t spike_bit(const StepArgs& a, uint32_t hrow,
@@ -271,18 +297,32 @@ __device__ __forceinline__ void pull_item(const StepArgs& a, const PullItem& it,
   }
 }
 
-// Warp-level dispatch of delivery unit u: spikes first, then ELL tiles and items.
+// Delivery phase for one warp: push items gw, gw + nw, ... up to the first
+// slot not written this step (each delivered item is cleared), then the dense
+// pull units.  Returns the synapses walked by the push items.
 template <bool BF16>
-__device__ __forceinline__ uint32_t deliver_unit(const StepArgs& a, uint32_t u, uint32_t n_act,
-                                                 const uint2* list, const StepIdx& ix) {
-  if (u < n_act) return push_item<BF16>(a, __ldcg(list + u), ix.slot);
-  u -= n_act;
-  if (u < a.n_pull_tiles) {
-    pull_tile<BF16>(a, a.pull_tiles[u], ix);
-    return 0;
+__device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw, uint32_t nw,
+                                                 const StepIdx& ix) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t walked = 0;
+  if (a.any_push) {
+    uint2* list = a.items + (size_t)(ix.t & 1) * a.item_cap;
+    const uint32_t tag = item_tag(ix.t);
+    for (uint32_t u = gw; u < a.item_cap; u += nw) {
+      const uint2 it = __ldcg(list + u);
+      if ((it.y & 0x7FFFFFu) != tag) break;
+      if (lane == 0) __stcg(&list[u].y, 0u);
+      walked += push_item<BF16>(a, it, ix.slot);
+    }
   }
-  pull_item<BF16>(a, a.pull_items[u - a.n_pull_tiles], ix);
-  return 0;
+  const uint32_t n_pull = a.n_pull_tiles + a.n_pull_items;
+  for (uint32_t u = gw; u < n_pull; u += nw) {
+    if (u < a.n_pull_tiles)
+      pull_tile<BF16>(a, a.pull_tiles[u], ix);
+    else
+      pull_item<BF16>(a, a.pull_items[u - a.n_pull_tiles], ix);
+  }
+  return walked;
 }
 
 __device__ __forceinline__ StepIdx step_of(const Ctl* ctl) {
@@ -314,14 +354,9 @@ template <bool BF16>
 __global__ void __launch_bounds__(kBlock) k_deliver(StepArgs a) {
   Ctl* ctl = a.ctl;
   const StepIdx ix = step_of(ctl);
-  const uint32_t n_act = a.any_push ? ctl->active_count[ix.t & 1] : 0u;
-  const uint2* list = a.items + (size_t)(ix.t & 1) * a.item_cap;
-  const uint32_t n_units = n_act + a.n_pull_tiles + a.n_pull_items;
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t nw = (gridDim.x * kBlock) >> 5;
-  uint32_t walked = 0;
-  for (uint32_t u = (blockIdx.x * kBlock + threadIdx.x) >> 5; u < n_units; u += nw)
-    walked += deliver_unit<BF16>(a, u, n_act, list, ix);
+  const uint32_t walked = deliver_warp<BF16>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5,
+                                             (gridDim.x * kBlock) >> 5, ix);
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   // Step bookkeeping by the last block to arrive.
   __shared__ bool last;
@@ -410,19 +445,79 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
   for (uint32_t s = 0; s < n_steps; ++s) {
     ix.t = t0 + s;
     ix.rel = s;
-    // Buffer of step t + 1: its last reader was the delivery of step t - 1.
+    // Item counter of step t + 1: its last user was the update of step t - 1.
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
     for (uint32_t u = gw; u < a.n_upd_words; u += nw) update_word(a, __ldg(a.upd_words + u), ix);
     if (!grid_barrier(a, target)) return;
     if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
-    const uint32_t n_act = a.any_push ? __ldcg(&ctl->active_count[ix.t & 1]) : 0u;
-    const uint2* list = a.items + (size_t)(ix.t & 1) * a.item_cap;
-    const uint32_t n_units = n_act + a.n_pull_tiles + a.n_pull_items;
-    for (uint32_t u = gw; u < n_units; u += nw) walked += deliver_unit<BF16>(a, u, n_act, list, ix);
+    walked += deliver_warp<BF16>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
     ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
   }
+  if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
+  if (leader) {
+    ctl->step = t0 + n_steps;
+    ctl->ring_slot = ix.slot;
+    ctl->hist_row = ix.hrow;
+    ctl->t_rel = n_steps;
+  }
+}
+
+// Resident form for networks with at most one 32-cell word per warp: each warp
+// keeps its cells' state, source masks, out-degrees and push-row bounds in
+// registers for the whole chunk and writes the state back at the end, so a
+// step's critical path is the ring read, the cell update and the deliveries.
+template <bool BF16>
+__global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepArgs a,
+                                                                          uint32_t n_steps) {
+  Ctl* ctl = a.ctl;
+  StepIdx ix = step_of(ctl);
+  const unsigned long long t0 = ix.t;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kPersistBlock) >> 5;
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool has = gw < a.n_upd_words;
+  uint32_t w = 0, seg = 0, i = 0, local = 0, mask = 0, r0 = 0, r1 = 0, od = 0;
+  bool valid = false, lif = false;
+  float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (has) {
+    w = __ldg(a.upd_words + gw);
+    seg = __ldg(a.seg_of_word + w);
+    i = (w << 5) + lane;
+    const SegDev& sd = a.segs[seg];
+    local = i - sd.base;
+    valid = local < sd.count;
+    lif = sd.kind == kSegLif;
+    if (valid) {
+      if (lif) st = a.state[i]; else mask = __ldg(a.src_mask + i);
+      od = __ldg(a.outdeg + i);
+      if (a.any_push) {
+        r0 = __ldg(a.push_row + i);
+        r1 = __ldg(a.push_row + i + 1);
+      }
+    }
+  }
+  unsigned long long target = 0;
+  uint32_t walked = 0;
+  for (uint32_t s = 0; s < n_steps; ++s) {
+    ix.t = t0 + s;
+    ix.rel = s;
+    if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
+    if (has) {
+      const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
+      publish_word(a, w, seg, i, fired, r0, r1, od, ix);
+    }
+    if (!grid_barrier(a, target)) break;
+    if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
+    walked += deliver_warp<BF16>(a, gw, nw, ix);
+    if (!grid_barrier(a, target)) break;
+    ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+    ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+  }
+  if (valid && lif) a.state[i] = st;
+  if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
     ctl->step = t0 + n_steps;
@@ -460,19 +555,26 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
 }
 
 int persistent_blocks_per_sm(bool bf16) {
-  int n = 0;
-  if (bf16)
+  int n = 0, m = 0;
+  if (bf16) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true>, kPersistBlock, 0);
-  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
+  } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, kPersistBlock, 0);
-  return n;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
+  }
+  return n < m ? n : m;
 }
 
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s) {
   StepArgs args = a;
   uint32_t n = n_steps;
   void* params[] = {&args, &n};
-  const void* fn = a.bf16 ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+  const bool resident = (uint64_t)a.n_upd_words * 32u <= (uint64_t)blocks * kPersistBlock;
+  const void* fn = resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
+                                      : (const void*)k_persistent_resident<false>)
+                            : (a.bf16 ? (const void*)k_persistent<true>
+                                      : (const void*)k_persistent<false>);
   return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, 0, s);
 }
 
