@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/scaffold_gb300.h"
 #include "sgb_device.h"
 #include "sgb_model.h"
@@ -120,5 +122,67 @@ extern "C" int sgb_deliver_spikes(const uint8_t* spikes, int32_t n_cells, const 
   cudaError_t e2 = cudaFreeAsync(scratch, st);
   if (e) return set_error(SGB_ERR_CUDA, "delivery launch failed: %s", cudaGetErrorString(e));
   if (e2) return set_error(SGB_ERR_CUDA, "cudaFreeAsync: %s", cudaGetErrorString(e2));
+  return SGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Delivery without any device allocation.
+//
+// Some callers cannot allocate device memory at the point where they deliver
+// spikes: a real-time loop in which a cudaMalloc (which may synchronise the
+// device) would break the step deadline, or a host process whose device
+// memory is owned by another allocator (a framework's caching allocator, a
+// fixed memory budget) that must not be bypassed.  sgb_deliver_spikes_static
+// gives them the same operation as sgb_deliver_spikes with its scratch (one
+// count word plus the active-cell list) in the file-scope array below, which
+// every GPU that loads this library holds until the process exits.
+static constexpr uint32_t kStaticMaxCells = 1u << 20;  // 1,048,576 cells: 4 MiB of scratch
+static __device__ __align__(256) uint32_t g_deliver_scratch[sgb::kListOffset + kStaticMaxCells];
+
+namespace sgb {
+namespace {
+
+constexpr int kMaxDevices = 64;
+
+std::mutex g_scratch_mu;
+uint32_t* g_scratch_addr[kMaxDevices] = {};
+
+// Device address of the static scratch on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked up
+// once per device, with that device current, and cached.
+int static_scratch(uint32_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e) return set_error(SGB_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(SGB_ERR_UNSUPPORTED, "device %d", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_deliver_scratch);
+    if (e) return set_error(SGB_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_scratch_addr[dev] = (uint32_t*)p;
+  }
+  *out = g_scratch_addr[dev];
+  return SGB_OK;
+}
+
+}  // namespace
+}  // namespace sgb
+
+extern "C" int sgb_deliver_spikes_static(const uint8_t* spikes, int32_t n_cells,
+                                         const uint32_t* row, const uint32_t* syn,
+                                         const void* weights, int32_t weight_type, int32_t* ring,
+                                         int32_t ring_slots, int64_t step, void* stream) {
+  if (n_cells > 0 && (uint32_t)n_cells > kStaticMaxCells)
+    return set_error(SGB_ERR_RANGE, "n_cells %d exceeds the static scratch of %u cells", n_cells,
+                     kStaticMaxCells);
+  int rc = deliver_check(n_cells, weight_type, ring_slots, step, spikes, row, syn, weights, ring);
+  if (rc) return rc;
+  uint32_t* scratch = nullptr;
+  rc = static_scratch(&scratch);
+  if (rc) return rc;
+  const cudaError_t e = deliver_enqueue(spikes, n_cells, row, syn, weights, weight_type, ring,
+                                        ring_slots, step, scratch, (cudaStream_t)stream);
+  if (e) return set_error(SGB_ERR_CUDA, "delivery launch failed: %s", cudaGetErrorString(e));
   return SGB_OK;
 }

@@ -124,6 +124,7 @@ PROTOTYPES = {
     "sgb_sim_launch_count": (C.c_int, [vp, i64p]),
     "sgb_sim_profile": (C.c_int, [vp, i32, f64p, f64p, i64p]),
     "sgb_deliver_spikes": (C.c_int, [vp, i32, vp, vp, vp, i32, vp, i32, i64, vp]),
+    "sgb_deliver_spikes_static": (C.c_int, [vp, i32, vp, vp, vp, i32, vp, i32, i64, vp]),
 }
 
 _lib = None

@@ -306,6 +306,25 @@ int sgb_deliver_spikes(const uint8_t* spikes, int32_t n_cells, const uint32_t* r
                        const uint32_t* syn, const void* weights, int32_t weight_type,
                        int32_t* ring, int32_t ring_slots, int64_t step, void* stream);
 
+/* Same operation as sgb_deliver_spikes, allocating nothing.  This entry point
+ * has no counterpart in the reference.  It is for callers that cannot
+ * allocate device memory when they deliver spikes: a real-time step loop in
+ * which a device allocation (which may synchronise the device) would break
+ * the deadline, or a process whose device memory belongs to another allocator
+ * (a framework's caching allocator, a fixed budget) that must not be bypassed.
+ * The caller passes inputs and outputs as above; the scratch (one count word
+ * and the list of active cells) is a file-scope device array of the library,
+ * sized for n_cells <= 1,048,576 (4 MiB), which every GPU that loads the
+ * library holds until the process exits.  Larger n_cells return
+ * SGB_ERR_RANGE.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current; make that first
+ * call before any stream capture.  Every call clears the count word on its
+ * stream and shares the one array, so calls that overlap on the GPU (other
+ * streams, other host threads) race: serialise them. */
+int sgb_deliver_spikes_static(const uint8_t* spikes, int32_t n_cells, const uint32_t* row,
+                              const uint32_t* syn, const void* weights, int32_t weight_type,
+                              int32_t* ring, int32_t ring_slots, int64_t step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
