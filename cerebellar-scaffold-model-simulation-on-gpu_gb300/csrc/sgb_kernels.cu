@@ -193,27 +193,78 @@ __device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint
   }
 }
 
-// General form: everything read from global memory.
-__device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
+// General form, everything from global memory.  The word's state and ring
+// slot are loaded first (their addresses depend only on the word index), the
+// segment descriptor next; push-row bounds and out-degrees only for spiking
+// cells.  Callers may issue load_word for the next word before finishing the
+// current one (the two touch different cells).
+struct WordIn {
+  float4 st;
+  int2 acc;
+  uint32_t seg;
+};
+
+__device__ __forceinline__ WordIn load_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
+  const uint32_t i = (w << 5) + (threadIdx.x & 31u);
+  WordIn in;
+  in.seg = __ldg(a.seg_of_word + w);
+  in.acc = __ldcg(reinterpret_cast<const int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i);
+  in.st = a.state[i];
+  return in;
+}
+
+__device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
+                                            const StepIdx& ix) {
+  if (in.seg == 0xFFFFu) return;  // padding between segments (warp-uniform)
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t seg = __ldg(a.seg_of_word + w);
-  const SegDev& sd = a.segs[seg];
+  const SegDev& sd = a.segs[in.seg];
   const uint32_t i = (w << 5) + lane;
   const uint32_t local = i - sd.base;
   const bool valid = local < sd.count;
-  uint32_t mask = 0, r0 = 0, r1 = 0, od = 0;
-  float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool fired = false;
   if (valid) {
-    if (sd.kind == kSegInput) mask = __ldg(a.src_mask + i); else st = a.state[i];
+    if (sd.kind == kSegInput) {
+      const uint32_t mask = __ldg(a.src_mask + i);
+      if (mask) fired = input_fire(a, sd, local, mask, ix.t);
+    } else {
+      if (in.acc.x | in.acc.y)
+        __stcg(reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i, make_int2(0, 0));
+      float4 st = in.st;
+      fired = lif_update(sd, a.substeps, st, in.acc);
+      a.state[i] = st;
+    }
+  }
+  uint32_t r0 = 0, r1 = 0, od = 0;
+  if (fired) {
     od = __ldg(a.outdeg + i);
     if (a.any_push) {
       r0 = __ldg(a.push_row + i);
       r1 = __ldg(a.push_row + i + 1);
     }
   }
-  const bool fired = cell_fire(a, sd, i, local, valid, st, mask, ix);
-  if (valid && sd.kind == kSegLif) a.state[i] = st;
-  publish_word(a, w, seg, i, fired, r0, r1, od, ix);
+  publish_word(a, w, in.seg, i, fired, r0, r1, od, ix);
+}
+
+__device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
+  finish_word(a, w, load_word(a, w, ix), ix);
+}
+
+// Words gw, gw + nw, ... with the next word's loads in flight while the
+// current one is computed.
+__device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uint32_t nw,
+                                             const StepIdx& ix) {
+  uint32_t w = gw;
+  if (w >= a.n_words) return;
+  WordIn cur = load_word(a, w, ix);
+  while (true) {
+    const uint32_t wn = w + nw;
+    WordIn nxt;
+    if (wn < a.n_words) nxt = load_word(a, wn, ix);
+    finish_word(a, w, cur, ix);
+    if (wn >= a.n_words) break;
+    w = wn;
+    cur = nxt;
+  }
 }
 
 // ---- phase 2: deliveries ------------------------------------------------------
@@ -342,10 +393,10 @@ __global__ void k_chunk_begin(StepArgs a) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_update(StepArgs a) {
-  const uint32_t u = (blockIdx.x * kBlock + threadIdx.x) >> 5;
-  if (u >= a.n_upd_words) return;
+  const uint32_t w = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  if (w >= a.n_words) return;
   const StepIdx ix = step_of(a.ctl);
-  update_word(a, __ldg(a.upd_words + u), ix);
+  update_word(a, w, ix);
 }
 
 // Delivery of step t; the last block to finish also advances the step
@@ -447,7 +498,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     ix.rel = s;
     // Item counter of step t + 1: its last user was the update of step t - 1.
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
-    for (uint32_t u = gw; u < a.n_upd_words; u += nw) update_word(a, __ldg(a.upd_words + u), ix);
+    update_words(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
     if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     walked += deliver_warp<BF16>(a, gw, nw, ix);
@@ -527,6 +578,126 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
   }
 }
 
+// Fused form (resident networks whose projections are all event-driven): a
+// step's deliveries only target ring slots t+1 .. t+D-1 while its update only
+// reads slot t, so update and push of the same step share one phase and a
+// step needs one grid barrier.  Each block gathers the push items of its
+// spiking cells in shared memory, so the rows of a cell with thousands of
+// synapses spread over the block's 32 warps.
+constexpr uint32_t kBlockItems = 2048;  // push items per block and step (16 KiB)
+
+template <bool BF16>
+__global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs a,
+                                                                       uint32_t n_steps) {
+  __shared__ uint2 s_items[kBlockItems];
+  __shared__ uint32_t s_n;
+  Ctl* ctl = a.ctl;
+  StepIdx ix = step_of(ctl);
+  const unsigned long long t0 = ix.t;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wib = threadIdx.x >> 5;
+  const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool has = gw < a.n_upd_words;
+  uint32_t w = 0, seg = 0, i = 0, local = 0, mask = 0, r0 = 0, r1 = 0, od = 0;
+  bool valid = false, lif = false;
+  float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (has) {
+    w = __ldg(a.upd_words + gw);
+    seg = __ldg(a.seg_of_word + w);
+    i = (w << 5) + lane;
+    const SegDev& sd = a.segs[seg];
+    local = i - sd.base;
+    valid = local < sd.count;
+    lif = sd.kind == kSegLif;
+    if (valid) {
+      if (lif) st = a.state[i]; else mask = __ldg(a.src_mask + i);
+      od = __ldg(a.outdeg + i);
+      r0 = __ldg(a.push_row + i);
+      r1 = __ldg(a.push_row + i + 1);
+    }
+  }
+  unsigned long long target = 0;
+  uint32_t walked = 0;
+  uint32_t s = 0;
+  for (; s < n_steps; ++s) {
+    ix.t = t0 + s;
+    ix.rel = s;
+    if (threadIdx.x == 0) s_n = 0;
+    if (leader && s > 0) a.raster_off[s] = __ldcg(&ctl->raster_count);
+    __syncthreads();
+    uint32_t off = 0, nit = 0;
+    if (has) {
+      const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
+      const uint32_t ballot = __ballot_sync(kFull, fired);
+      if (lane == 0) __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, ballot);
+      if (ballot) {
+        const uint32_t n = __popc(ballot);
+        const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
+        const uint32_t ev = __reduce_add_sync(kFull, fired ? od : 0u);
+        nit = fired ? (r1 - r0 + kPushChunk - 1) / kPushChunk : 0u;
+        uint32_t incl = nit;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t v = __shfl_up_sync(kFull, incl, o);
+          if (lane >= (uint32_t)o) incl += v;
+        }
+        const uint32_t tot = __shfl_sync(kFull, incl, 31);
+        uint32_t roff = 0;
+        if (lane == 0) {
+          if (tot) off = atomicAdd(&s_n, tot);
+          atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], n);
+          if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
+          if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
+        }
+        off = __shfl_sync(kFull, off, 0) + incl - nit;
+        for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
+          const uint32_t q0 = r0 + k * kPushChunk;
+          s_items[off + k] = make_uint2(q0, min(kPushChunk, r1 - q0) << 23);
+        }
+        if (a.raster_cap) {
+          roff = __shfl_sync(kFull, roff, 0);
+          if (fired) {
+            if (roff + rank < a.raster_cap)
+              a.raster[roff + rank] = i;
+            else
+              atomicOr(&ctl->error, kErrRasterOverflow);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t n_items = min(s_n, kBlockItems);
+    for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32)
+      walked += push_item<BF16>(a, s_items[u], ix.slot);
+    // Items beyond the block's capacity are delivered by the warp that made them.
+    uint32_t spill = __ballot_sync(kFull, off + nit > kBlockItems);
+    while (spill) {
+      const int src = __ffs(spill) - 1;
+      spill &= spill - 1;
+      const uint32_t o = __shfl_sync(kFull, off, src), c = __shfl_sync(kFull, nit, src);
+      const uint32_t b0 = __shfl_sync(kFull, r0, src), b1 = __shfl_sync(kFull, r1, src);
+      for (uint32_t k = o < kBlockItems ? kBlockItems - o : 0; k < c; ++k) {
+        const uint32_t q0 = b0 + k * kPushChunk;
+        walked += push_item<BF16>(a, make_uint2(q0, min(kPushChunk, b1 - q0) << 23), ix.slot);
+      }
+    }
+    if (!grid_barrier(a, target)) break;
+    ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+    ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+  }
+  if (valid && lif) a.state[i] = st;
+  if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
+  if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
+  if (leader) {
+    a.raster_off[n_steps] = __ldcg(&ctl->raster_count);
+    ctl->step = t0 + n_steps;
+    ctl->ring_slot = ix.slot;
+    ctl->hist_row = ix.hrow;
+    ctl->t_rel = n_steps;
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_chunk_begin(const StepArgs& a, cudaStream_t s) {
@@ -536,7 +707,7 @@ cudaError_t launch_chunk_begin(const StepArgs& a, cudaStream_t s) {
 
 cudaError_t launch_update(const StepArgs& a, cudaStream_t s) {
   if (!a.n_upd_words) return cudaSuccess;
-  k_update<<<(a.n_upd_words + kBlock / 32 - 1) / (kBlock / 32), kBlock, 0, s>>>(a);
+  k_update<<<(a.n_words + kBlock / 32 - 1) / (kBlock / 32), kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -556,14 +727,18 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
 
 int persistent_blocks_per_sm(bool bf16) {
   int n = 0, m = 0;
+  int f = 0;
   if (bf16) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<true>, kPersistBlock, 0);
   } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<false>, kPersistBlock, 0);
   }
-  return n < m ? n : m;
+  n = n < m ? n : m;
+  return n < f ? n : f;
 }
 
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s) {
@@ -571,10 +746,13 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
   uint32_t n = n_steps;
   void* params[] = {&args, &n};
   const bool resident = (uint64_t)a.n_upd_words * 32u <= (uint64_t)blocks * kPersistBlock;
-  const void* fn = resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
-                                      : (const void*)k_persistent_resident<false>)
-                            : (a.bf16 ? (const void*)k_persistent<true>
-                                      : (const void*)k_persistent<false>);
+  const bool fused = resident && a.n_pull_tiles == 0 && a.n_pull_items == 0;
+  const void* fn = fused      ? (a.bf16 ? (const void*)k_persistent_fused<true>
+                                        : (const void*)k_persistent_fused<false>)
+                   : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
+                                        : (const void*)k_persistent_resident<false>)
+                              : (a.bf16 ? (const void*)k_persistent<true>
+                                        : (const void*)k_persistent<false>);
   return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, 0, s);
 }
 
