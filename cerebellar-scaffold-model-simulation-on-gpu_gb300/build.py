@@ -33,6 +33,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 SOURCES = [
     ("sgb_model.cpp", "cxx"),
     ("sgb_capi.cpp", "cxx"),
+    ("sgb_compat.cpp", "cxx"),
     ("sgb_engine.cu", "nvcc"),
     ("sgb_kernels.cu", "nvcc"),
     ("sgb_ops.cu", "nvcc"),
@@ -50,7 +51,8 @@ def _newer(target: str, deps: list[str]) -> bool:
 def _compile(src: str, kind: str) -> str:
     path = os.path.join(CSRC, src)
     obj = os.path.join(BUILD, src + ".o")
-    deps = [path] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "scaffold_gb300.h")]
+    deps = [path] + [os.path.join(CSRC, h) for h in HEADERS] + [
+        os.path.join(INCLUDE, "scaffold_gb300.h"), os.path.join(INCLUDE, "scaffold_compat.h")]
     if not _newer(obj, deps):
         return obj
     if kind == "cxx":

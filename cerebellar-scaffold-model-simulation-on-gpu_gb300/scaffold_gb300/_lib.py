@@ -98,6 +98,9 @@ PROTOTYPES = {
     "sgb_net_add_input": (C.c_int, [vp, i32, i64, u32p, P(InputParams), i32p]),
     "sgb_net_add_input_dat": (C.c_int, [vp, C.c_char_p, i32, P(InputParams), i32p]),
     "sgb_net_build_scaffold": (C.c_int, [vp, i32, f64, u64]),
+    "sgb_net_build_reference_scaffold": (C.c_int, [vp, C.c_char_p, i32p]),
+    "sgb_reference_type_id": (i32, [i32]),
+    "sgb_sim_write_raster": (C.c_int, [vp, C.c_char_p, u32p, i64p, i64, i64, i32p, i32]),
     "sgb_net_counts": (C.c_int, [vp, i32p, i32p, i32p, i64p, i64p]),
     "sgb_net_population_info": (C.c_int, [vp, i32, P(PopulationInfo)]),
     "sgb_net_projection_info": (C.c_int, [vp, i32, P(ProjectionInfo)]),

@@ -301,6 +301,19 @@ class Simulation:
             r = (ids[: offs[-1]].copy(), offs)
         return cnt, r
 
+    def write_raster(self, path: str, ids, offsets, first_step: int = 0, type_ids=None,
+                     append: bool = False) -> None:
+        """Raster in the reference's text format ("t\tlocal_id\ttype_id" lines)."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        tids = None
+        if type_ids is not None:
+            tids = np.ascontiguousarray(type_ids, dtype=np.int32)
+        L.check(L.lib().sgb_sim_write_raster(
+            self._h, path.encode(), _ptr(ids, C.c_uint32), _ptr(offsets, C.c_int64),
+            len(offsets) - 1, first_step, _ptr(tids, C.c_int32) if tids is not None else None,
+            1 if append else 0))
+
     def run(self, n_steps: int) -> None:
         """Advances without host outputs (device-resident run)."""
         L.check(L.lib().sgb_sim_run(self._h, n_steps, None, None, 0, None))

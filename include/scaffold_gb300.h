@@ -198,6 +198,22 @@ int sgb_net_add_input_dat(sgb_net* net, const char* path, int32_t pop,
  * (init_params.cu:367-766) for the synthetic workloads. */
 int sgb_net_build_scaffold(sgb_net* net, int32_t config, double scale, uint64_t seed);
 
+/* Reference-structure mode: the reference's hard-coded scaffold (populations
+ * and parameters of init_neurons_params, the 16 projections, weights and ms
+ * delays of init_connectivity_params; init_params.cu:367-766) over the .dat
+ * files in `dat_dir` (the reference's file names and format), and its two
+ * stimulus lists background_noise.dat (Poisson 1 Hz) and tone_stim.dat
+ * (periodic 140 Hz from 292.8 ms within [300, 351) ms, or Poisson 1 Hz;
+ * UserInputFunctions.cu:19-29,72-81).  Delays in ms are exchange steps, as
+ * with the reference's 1-ms step (cfg.dt_ms = 0.1, cfg.substeps = 10).
+ * Populations are in the reference's array order (granule, purkinje, golgi,
+ * stellate, basket, dcn, glomerulus); `sizes` (NULL: the reference's)
+ * overrides the population sizes. */
+int sgb_net_build_reference_scaffold(sgb_net* net, const char* dat_dir, const int32_t* sizes);
+/* NeuronType enum value (struct_enum_def.h:10-20) of population `pop` of the
+ * reference scaffold, as the reference prints it in rasters; -1 if none. */
+int32_t sgb_reference_type_id(int32_t pop);
+
 int sgb_net_counts(const sgb_net* net, int32_t* n_pops, int32_t* n_projs, int32_t* n_inputs,
                    int64_t* n_neurons, int64_t* n_synapses);
 int sgb_net_population_info(const sgb_net* net, int32_t pop, sgb_population_info* info);
@@ -263,6 +279,15 @@ int sgb_sim_segment_info(const sgb_sim* sim, int32_t seg, sgb_segment_info* info
  * (any pointer may be NULL).  INPUT cells report zeros. */
 int sgb_sim_get_state(sgb_sim* sim, float* u, float* g, int32_t* ref);
 int sgb_sim_set_state(sgb_sim* sim, const float* u, const float* g, const int32_t* ref);
+
+/* Writes a raster returned by sgb_sim_run in the reference's text format,
+ * one "t\tlocal_id\ttype_id" line per spike (print_spike_train,
+ * GPUScaffoldSimulation.cu:77-85): t in ms as %f (step index first_step + k
+ * times the exchange step), the cell's index within its population, and
+ * type_ids[population] (NULL: the population index). */
+int sgb_sim_write_raster(const sgb_sim* sim, const char* path, const uint32_t* ids,
+                         const int64_t* offsets, int64_t n_steps, int64_t first_step,
+                         const int32_t* type_ids, int32_t append);
 
 /* Long-horizon spike totals per segment (FP64 accumulators, updated on the
  * device at the end of every chunk). */
