@@ -50,6 +50,7 @@ def parse():
                     help="exchange steps of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec", default="persistent", choices=["persistent", "graph"])
+    ap.add_argument("--no-ell-roofline", action="store_true")
     ap.add_argument("--blocks-per-sm", type=int, default=1)
     return ap.parse_args()
 
@@ -175,6 +176,28 @@ def cpu_baseline(wl: dict, sample_steps: int):
                       f"OpenMP over post cells"}
 
 
+def ell_roofline(peak: float):
+    """Dense ELL pull at HBM scale: the ~925k-cell config-5 scaffold (27.3M
+    synapses; BF16 ELL tables of ~164 MB, larger than L2) with every projection
+    forced to dense pull; delivery-kernel time from CUDA events per launch."""
+    import scaffold_gb300 as sg
+
+    net = sg.scaffold(5, 1.0, 1)
+    sim = sg.Simulation([net], [1], weight_type=sg.WEIGHT_BF16, chunk_steps=100,
+                        exec_mode=sg.EXEC_GRAPH)
+    for j in range(len(net.projections)):
+        sim.set_propagation(0, j, sg.PROP_ELL)
+    sim.run(20)
+    mean_us, bytes_pl, nl = sim.profile(50)
+    info = sim.info()
+    sim.close()
+    gbs = bytes_pl[1] / (mean_us[1] * 1e-6) / 1e9
+    return {"kernel": "k_deliver (dense ELL pull, every projection)", "workload":
+            f"config 5: {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
+            "mean_us": mean_us[1], "bytes_per_launch": bytes_pl[1], "achieved": gbs,
+            "unit": "GB/s", "peak": peak, "frac": gbs / peak}
+
+
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -242,6 +265,7 @@ def run_gb300(a):
         sim.enqueue(a.chunk)
     sim.sync()
     ev0 = sim.info().events
+    dlv0 = sim.info().delivered
     l0 = sim.launch_count()
     clocks = Clocks(local)
     clocks.start()
@@ -264,7 +288,9 @@ def run_gb300(a):
         pg.barrier()
     clk = clocks.stop()
     ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
-    events = sim.info().events - ev0
+    info_t = sim.info()
+    events = info_t.events - ev0
+    dlv1 = info_t.delivered
     launches = sim.launch_count() - l0
     ms_max, events_all = aggregate(pg, "cuda", ms, float(events))
     value = realtime_factor(world, a.steps, bio_per_step, ms_max)
@@ -293,26 +319,40 @@ def run_gb300(a):
         if pg:
             pg.destroy_process_group()
         return
-    # Roofline of the dominant kernel from an instrumented run (CUDA events on
-    # the handle's stream around every launch).
-    mean_us, bytes_pl, nl = sim.profile(1000)
-    names = ["k_update", "k_deliver"]
-    share = [m * n for m, n in zip(mean_us, nl)]
-    dom = max(range(len(names)), key=lambda k: share[k])
+    # Roofline of the kernel that ran the timed region.  Algorithmic bytes:
+    # per LIF cell and step 16 B state read + 16 B write + 8 B ring slot; per
+    # input cell 4 B source mask; 4 B per 32-cell bitmap word; per delivered
+    # synapse 4 B word + W B weight + 8 B atomic read-modify-write.
+    segs = sim.segments()
+    n_lif = sum(sg_.count for sg_ in segs if sg_.dev_type != sg.INPUT)
+    n_in = sum(sg_.count for sg_ in segs if sg_.dev_type == sg.INPUT)
+    n_words = sum((sg_.count + 31) // 32 for sg_ in segs)
+    wbytes = 2 if wl["bf16"] else 4
+    info1 = sim.info()
+    upd_step = 40 * n_lif + 4 * n_in + 4 * n_words
+    alg_bytes = a.steps * a.chunk * upd_step + (dlv1 - dlv0) * (12 + wbytes)
     peak, peak_kind = measured_hbm()
-    achieved = bytes_pl[dom] / (mean_us[dom] * 1e-6) / 1e9 if mean_us[dom] > 0 else 0.0
+    achieved = alg_bytes / (ms / 1000.0) / 1e9
+    kname = sg._lib.KERNEL_NAMES.get(info1.step_kernel, "?")
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         try:
-            traffic = json.load(open(tp)).get(a.workload, {}).get(names[dom])
+            traffic = json.load(open(tp)).get(a.workload, {}).get(kname)
         except ValueError:
             traffic = None
-    roof = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
             "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "algorithmic_bytes_per_launch": bytes_pl[dom],
-            "mean_us_per_launch": mean_us[dom],
-            "kernel_time_share": {n: s / max(sum(share), 1e-12) for n, s in zip(names, share)}}
+            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes / a.steps,
+            "mean_us_per_launch": 1000.0 * ms / a.steps,
+            "launches_timed": a.steps, "steps_per_launch": a.chunk}
+    # Per-phase view from an instrumented run of the per-step kernels (CUDA
+    # events on the handle's stream around every launch).
+    mean_us, bytes_pl, nl = sim.profile(1000)
+    phases = {n: {"mean_us": m, "bytes_per_launch": b,
+                  "achieved_gbs": (b / (m * 1e-6) / 1e9) if m > 0 else 0.0}
+              for n, m, b in zip(["k_update", "k_deliver"], mean_us, bytes_pl)}
+    ell = None if a.no_ell_roofline else ell_roofline(peak)
     cpu = None
     if not a.no_cpu_baseline:
         try:
@@ -337,6 +377,8 @@ def run_gb300(a):
         "gpu_launches": launches,
         "e2e": e2e,
         "roofline": roof,
+        "phase_profile": phases,
+        "dense_ell_roofline": ell,
         "cpu_baseline": cpu,
         "clocks": clk,
     }

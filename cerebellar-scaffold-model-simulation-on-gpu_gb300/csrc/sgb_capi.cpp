@@ -290,6 +290,10 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
     return set_error(SGB_ERR_CUDA, "reading the step counter failed");
   info->step = (int64_t)ctl.step;
   info->events = (int64_t)ctl.events;
+  info->delivered = (int64_t)ctl.delivered;
+  info->step_kernel = s.cfg.exec_mode == SGB_EXEC_PERSISTENT
+                          ? persistent_kernel_kind(s.args, s.persistent_blocks)
+                          : SGB_KERNEL_GRAPH;
   info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;
   info->weight_type = s.cfg.weight_type;

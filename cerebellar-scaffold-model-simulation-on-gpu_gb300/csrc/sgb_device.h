@@ -146,5 +146,7 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s);
 // One cooperative launch advancing n_steps; grid = blocks (all co-resident).
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s);
 int persistent_blocks_per_sm(bool bf16);
+// Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
+int persistent_kernel_kind(const StepArgs& a, int blocks);
 
 }  // namespace sgb

@@ -741,12 +741,19 @@ int persistent_blocks_per_sm(bool bf16) {
   return n < f ? n : f;
 }
 
+int persistent_kernel_kind(const StepArgs& a, int blocks) {
+  const bool resident = (uint64_t)a.n_upd_words * 32u <= (uint64_t)blocks * kPersistBlock;
+  if (!resident) return SGB_KERNEL_GENERAL;
+  return a.n_pull_tiles == 0 && a.n_pull_items == 0 ? SGB_KERNEL_FUSED : SGB_KERNEL_RESIDENT;
+}
+
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s) {
   StepArgs args = a;
   uint32_t n = n_steps;
   void* params[] = {&args, &n};
-  const bool resident = (uint64_t)a.n_upd_words * 32u <= (uint64_t)blocks * kPersistBlock;
-  const bool fused = resident && a.n_pull_tiles == 0 && a.n_pull_items == 0;
+  const int kind = persistent_kernel_kind(a, blocks);
+  const bool resident = kind != SGB_KERNEL_GENERAL;
+  const bool fused = kind == SGB_KERNEL_FUSED;
   const void* fn = fused      ? (a.bf16 ? (const void*)k_persistent_fused<true>
                                         : (const void*)k_persistent_fused<false>)
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>

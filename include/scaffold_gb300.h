@@ -132,7 +132,16 @@ typedef struct sgb_sim_info {
   int32_t exec_mode, weight_type, substeps, chunk_steps;
   double dt_ms;
   int64_t events;        /* synaptic events (spikes x out-degree) since the last reset */
+  int64_t delivered;     /* synapses walked by event-driven delivery since the last reset */
+  int32_t step_kernel;   /* SGB_KERNEL_*: the kernel a chunk of steps runs in            */
+  int32_t reserved_;
 } sgb_sim_info;
+
+/* Step kernels (sgb_sim_info.step_kernel). */
+#define SGB_KERNEL_GRAPH 0      /* k_update + k_deliver per step, CUDA graph or stream */
+#define SGB_KERNEL_GENERAL 1    /* persistent, two grid barriers per step              */
+#define SGB_KERNEL_RESIDENT 2   /* persistent, state in registers, two barriers        */
+#define SGB_KERNEL_FUSED 3      /* persistent, state in registers, one barrier         */
 
 typedef struct sgb_net sgb_net;
 typedef struct sgb_sim sgb_sim;
