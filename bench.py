@@ -33,6 +33,9 @@ WORKLOADS = {
                desc="config 4: 64 config-2 instances scaled U[0.25,2.0], BF16, batched"),
     "c1": dict(config=1, scale=1.0, instances=1, bf16=False,
                desc="config 1: 9,256-cell net, 196,960 synapses, FP32"),
+    "c5": dict(config=5, scale=1.0, instances=4, bf16=True, autotune=True,
+               desc="config 5: 4 seeds of the ~925k-cell scaffold (10x config 2), BF16, "
+                    "batched, propagation mode per projection from the autotuner"),
 }
 
 
@@ -46,12 +49,14 @@ def parse():
     ap.add_argument("--chunk", type=int, default=1000, help="exchange steps per bench step")
     ap.add_argument("--ref-sample", type=int, default=100,
                     help="exchange steps per bench step of the reference arm")
-    ap.add_argument("--cpu-sample", type=int, default=1000,
+    ap.add_argument("--cpu-sample", type=int, default=20000,
                     help="exchange steps of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec", default="persistent", choices=["persistent", "graph"])
     ap.add_argument("--no-ell-roofline", action="store_true")
     ap.add_argument("--blocks-per-sm", type=int, default=1)
+    ap.add_argument("--autotune", action="store_true",
+                    help="run the propagation/driver autotuner before timing (default for c5)")
     return ap.parse_args()
 
 
@@ -177,25 +182,30 @@ def cpu_baseline(wl: dict, sample_steps: int):
 
 
 def ell_roofline(peak: float):
-    """Dense ELL pull at HBM scale: the ~925k-cell config-5 scaffold (27.3M
-    synapses; BF16 ELL tables of ~164 MB, larger than L2) with every projection
-    forced to dense pull; delivery-kernel time from CUDA events per launch."""
+    """Dense ELL pull at HBM scale: config 5 (4 batched seeds of the ~925k-cell
+    scaffold, 109M synapses, 437 MB of ELL entries, larger than L2) with every
+    projection forced to dense pull; k_pull time from CUDA events per launch.
+    Algorithmic bytes: 4 B per stored entry, plus W + 8 B per entry whose pre
+    cell spiked (weight and ring atomic)."""
     import scaffold_gb300 as sg
 
-    net = sg.scaffold(5, 1.0, 1)
-    sim = sg.Simulation([net], [1], weight_type=sg.WEIGHT_BF16, chunk_steps=100,
+    seeds = [1, 2, 3, 4]
+    nets = [sg.scaffold(5, 1.0, sd) for sd in seeds]
+    sim = sg.Simulation(nets, seeds, weight_type=sg.WEIGHT_BF16, chunk_steps=100,
                         exec_mode=sg.EXEC_GRAPH)
-    for j in range(len(net.projections)):
-        sim.set_propagation(0, j, sg.PROP_ELL)
+    for k, net in enumerate(nets):
+        for j in range(len(net.projections)):
+            sim.set_propagation(k, j, sg.PROP_ELL)
     sim.run(20)
     mean_us, bytes_pl, nl = sim.profile(50)
     info = sim.info()
     sim.close()
-    gbs = bytes_pl[1] / (mean_us[1] * 1e-6) / 1e9
-    return {"kernel": "k_deliver (dense ELL pull, every projection)", "workload":
-            f"config 5: {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
-            "mean_us": mean_us[1], "bytes_per_launch": bytes_pl[1], "achieved": gbs,
-            "unit": "GB/s", "peak": peak, "frac": gbs / peak}
+    gbs = bytes_pl[2] / (mean_us[2] * 1e-6) / 1e9
+    return {"kernel": "k_pull (dense ELL pull, every projection)", "workload":
+            f"config 5: 4 seeds, {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
+            "mean_us": mean_us[2], "bytes_per_launch": bytes_pl[2], "achieved": gbs,
+            "unit": "GB/s", "peak": peak, "frac": gbs / peak,
+            "l2": "entries 437 MB per launch (not L2-resident); no flush between launches"}
 
 
 def run_reference(a):
@@ -257,6 +267,12 @@ def run_gb300(a):
                         blocks_per_sm=a.blocks_per_sm)
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
+    tuned = None
+    if a.autotune or wl.get("autotune"):
+        sim.autotune(100)
+        modes = [sim.get_propagation(0, j) for j in range(len(nets[0].projections))]
+        tuned = {"ell": sum(m == sg.PROP_ELL for m in modes), "csr": sum(m == sg.PROP_CSR
+                                                                     for m in modes)}
     info = sim.info()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     bio_per_step = a.chunk * 0.1e-3 * len(nets)
@@ -266,6 +282,7 @@ def run_gb300(a):
     sim.sync()
     ev0 = sim.info().events
     dlv0 = sim.info().delivered
+    pull0 = sim.info().pulled
     l0 = sim.launch_count()
     clocks = Clocks(local)
     clocks.start()
@@ -321,16 +338,19 @@ def run_gb300(a):
         return
     # Roofline of the kernel that ran the timed region.  Algorithmic bytes:
     # per LIF cell and step 16 B state read + 16 B write + 8 B ring slot; per
-    # input cell 4 B source mask; 4 B per 32-cell bitmap word; per delivered
-    # synapse 4 B word + W B weight + 8 B atomic read-modify-write.
+    # input cell 4 B source mask; 8 B per 32-cell bitmap word (two history
+    # copies); per delivered push synapse 4 B word + W B weight + 8 B atomic
+    # read-modify-write; per dense entry and step 4 B, plus W + 8 B per entry
+    # whose pre cell spiked.
     segs = sim.segments()
     n_lif = sum(sg_.count for sg_ in segs if sg_.dev_type != sg.INPUT)
     n_in = sum(sg_.count for sg_ in segs if sg_.dev_type == sg.INPUT)
     n_words = sum((sg_.count + 31) // 32 for sg_ in segs)
     wbytes = 2 if wl["bf16"] else 4
     info1 = sim.info()
-    upd_step = 40 * n_lif + 4 * n_in + 4 * n_words
-    alg_bytes = a.steps * a.chunk * upd_step + (dlv1 - dlv0) * (12 + wbytes)
+    upd_step = 40 * n_lif + 4 * n_in + 8 * n_words + 4 * info_t.pull_entries
+    alg_bytes = (a.steps * a.chunk * upd_step + (dlv1 - dlv0) * (12 + wbytes) +
+                 (info_t.pulled - pull0) * (8 + wbytes))
     peak, peak_kind = measured_hbm()
     achieved = alg_bytes / (ms / 1000.0) / 1e9
     kname = sg._lib.KERNEL_NAMES.get(info1.step_kernel, "?")
@@ -351,7 +371,8 @@ def run_gb300(a):
     mean_us, bytes_pl, nl = sim.profile(1000)
     phases = {n: {"mean_us": m, "bytes_per_launch": b,
                   "achieved_gbs": (b / (m * 1e-6) / 1e9) if m > 0 else 0.0}
-              for n, m, b in zip(["k_update", "k_deliver"], mean_us, bytes_pl)}
+              for n, m, b, c in zip(["k_update", "k_deliver", "k_pull"], mean_us, bytes_pl, nl)
+              if c > 0}
     ell = None if a.no_ell_roofline else ell_roofline(peak)
     cpu = None
     if not a.no_cpu_baseline:
@@ -368,9 +389,13 @@ def run_gb300(a):
                    "instances_per_gpu": len(nets), "dt_ms": 0.1,
                    "steps_per_bench_step": a.chunk, "bio_s_per_bench_step": bio_per_step,
                    "weights": "bf16" if wl["bf16"] else "fp32",
-                   "exec": ("one persistent cooperative kernel per chunk" if a.exec == "persistent"
-                            else "cuda graph of 2 kernels per step"),
-                   "propagation": "event-driven CSR push",
+                   "exec": {sg.EXEC_PERSISTENT: "one persistent cooperative kernel per chunk",
+                            sg.EXEC_GRAPH: "cuda graph of 2 kernels per step"}.get(
+                                info.exec_mode, "per-step launches"),
+                   "propagation": ("event-driven CSR push" if tuned is None else
+                                   f"autotuned: {tuned['ell']} projections dense ELL pull, "
+                                   f"{tuned['csr']} event-driven CSR push (instance 0)"),
+                   "exec_kernel": sg._lib.KERNEL_NAMES.get(info.step_kernel, "?"),
                    "l2": "flushed (256 MiB write) between timed steps",
                    "parallelism": f"replicas x{world}"},
         "synaptic_events_per_s": events_all / (ms_max / 1000.0),

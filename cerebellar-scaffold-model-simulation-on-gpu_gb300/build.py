@@ -28,7 +28,8 @@ CXX = os.environ.get("CXX", "g++")
 HOST_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall",
               "-Wno-unused-function"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
+                     "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp",
+                     "--expt-relaxed-constexpr"]
 
 SOURCES = [
     ("sgb_model.cpp", "cxx"),

@@ -291,6 +291,9 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
   info->step = (int64_t)ctl.step;
   info->events = (int64_t)ctl.events;
   info->delivered = (int64_t)ctl.delivered;
+  info->pulled = (int64_t)ctl.pulled;
+  for (const ProjDev& P : s.projs)
+    if (P.mode == SGB_PROP_ELL) info->pull_entries += P.ell_n;
   info->step_kernel = s.cfg.exec_mode == SGB_EXEC_PERSISTENT
                           ? persistent_kernel_kind(s.args, s.persistent_blocks)
                           : SGB_KERNEL_GRAPH;

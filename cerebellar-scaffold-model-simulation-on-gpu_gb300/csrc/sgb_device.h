@@ -30,7 +30,9 @@ namespace sgb {
 constexpr int kBlock = 256;           // threads per block of the per-step kernels
 constexpr int kPersistBlock = 1024;   // threads per block of the persistent kernel
 constexpr uint32_t kPushChunk = 256;  // synapses per push work item (8 per lane)
-constexpr int kPullWarpChunk = 1024;  // synapses per warp item of the row-major ELL pull
+constexpr uint32_t kPullUnit = 1024;  // ELL entries per dense-pull work unit (32 per lane)
+constexpr int kPullBlock = 1024;             // threads per k_pull block (one per SM)
+constexpr size_t kPullSumMax = 192 * 1024;  // largest spike summary k_pull stages (H + 1 rows)
 constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-major layout
 // Push-table synapse word: 27-bit padded post index, 4-bit delay, 1-bit accumulator.
 constexpr uint32_t kPushPostBits = 27;
@@ -68,8 +70,8 @@ struct ProjDev {
   float scale;                    // 2^S of the post segment's accumulator
   uint32_t ell_K;                 // ELL width (max in-degree)
   uint32_t ell_rowmajor;          // 0: [K][post_count], 1: [post_count][K]
-  uint32_t pad_;
-  const uint32_t* ell_syn;        // pre | delay << 28, kEllPad for padding
+  uint32_t ell_n;                 // entries (ell_K * post_count)
+  const uint32_t* ell_syn;        // ell_entry words, ell_pad for padding
   const void* ell_w;              // weights x 2^S
 };
 
@@ -94,13 +96,14 @@ struct Ctl {
   unsigned long long barrier_arrive;
   unsigned long long events;      // synaptic events (spikes x out-degree) since reset
   unsigned long long delivered;   // synapses walked by the CSR push since reset
+  unsigned long long pulled;      // dense-pull entries whose pre cell spiked, since reset
 };
 
 constexpr uint32_t kErrRasterOverflow = 1u;
 constexpr uint32_t kErrBarrierTimeout = 2u;
 
-struct PullTile { uint32_t proj, post_start; };   // 32 posts of a column-major ELL
-struct PullItem { uint32_t proj, post, k0; };      // one row chunk of a row-major ELL
+// kPullUnit consecutive entries [o0, o0 + kPullUnit) of one projection's ELL.
+struct PullUnit { uint32_t proj, o0; };
 
 // Everything a step kernel needs, passed by value.
 struct StepArgs {
@@ -116,11 +119,12 @@ struct StepArgs {
   const uint32_t* push_row;       // [n_pad + 1] push-table row offsets
   const uint32_t* push_syn;
   const void* push_w;
-  const PullTile* pull_tiles;
-  const PullItem* pull_items;
+  const PullUnit* pull_units;
   float4* state;
   int* ring;                      // int2 per cell per slot, viewed as int[2]
-  uint32_t* hist;                 // [H][n_words]
+  uint32_t* hist;                 // [2H][n_words]: row r and r + H hold step r mod H
+  uint32_t* hsum;                 // [H + 1][n_swords]: bit w of row t mod (H + 1) = word w
+                                  // of step t had a spike
   uint2* items;                   // [2][item_cap] push work ranges
   uint32_t* counts;               // [chunk_steps][n_segs]
   uint32_t* raster;               // [raster_cap] padded ids
@@ -129,7 +133,10 @@ struct StepArgs {
   unsigned long long* bar;        // grid-barrier arrival counter (zeroed per launch)
   uint32_t n_pad, n_words, n_segs, n_projs;
   uint32_t ring_slots, hist_rows;
-  uint32_t n_upd_words, n_pull_tiles, n_pull_items;
+  uint32_t n_upd_words, n_pull_units;
+  uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
+  uint32_t ell_shift;             // ELL entry = (delay - 1) << ell_shift | cell
+  uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory
   uint32_t any_push;
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer
@@ -146,6 +153,12 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s);
 // One cooperative launch advancing n_steps; grid = blocks (all co-resident).
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s);
 int persistent_blocks_per_sm(bool bf16);
+// Dense pull (per-step driver): k_pull needs pull_setup() once per device
+// before its first launch.
+cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s);
+cudaError_t pull_setup();
+int pull_blocks_per_sm(const StepArgs& a);
+size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summary rows
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
 int persistent_kernel_kind(const StepArgs& a, int blocks);
 

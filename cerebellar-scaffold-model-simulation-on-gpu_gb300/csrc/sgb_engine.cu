@@ -111,11 +111,12 @@ static float scaled_weight(float w, int32_t bits, bool bf16) {
 
 // ---------------------------------------------------------------------------
 // Post-major ELL of one projection, width = max in-degree, padding at the end
-// of each row; column-major for narrow rows (one thread per post), row-major
-// for wide ones (one warp per row chunk).
-static void build_ell(const Projection& pr, int32_t npost, bool bf16, ProjTables& t,
-                      std::vector<uint32_t>& syn, std::vector<float>& wf,
-                      std::vector<uint16_t>& wh) {
+// of each row; column-major for narrow rows, row-major for wide ones (either
+// way the pull streams it as flat units, so the table is padded to whole
+// units).  Entries are ell_entry words (at most 2^27 padded cells).
+static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, uint32_t ell_shift,
+                      uint32_t pad, bool bf16, ProjTables& t, std::vector<uint32_t>& syn,
+                      std::vector<float>& wf, std::vector<uint16_t>& wh) {
   const size_t nnz = pr.pre_idx.size();
   std::vector<uint32_t> indeg((size_t)npost, 0);
   for (size_t i = 0; i < nnz; ++i) indeg[pr.post_idx[i]]++;
@@ -124,17 +125,39 @@ static void build_ell(const Projection& pr, int32_t npost, bool bf16, ProjTables
   t.ell_K = K;
   t.ell_rowmajor = K > kEllColMajorMaxK;
   const size_t cells = (size_t)K * (size_t)npost;
-  syn.assign(cells, kEllPad);
+  if (cells >= (1ull << 32) - kPullUnit) return false;  // entry offsets are 32-bit
+  syn.assign(align_up(cells, kPullUnit), pad);  // whole pull units
   if (bf16) wh.assign(cells, 0); else wf.assign(cells, 0.f);
-  std::vector<uint32_t> col((size_t)npost, 0);
-  for (size_t i = 0; i < nnz; ++i) {
-    const uint32_t p = pr.post_idx[i];
-    const uint32_t k = col[p]++;
-    const size_t q = t.ell_rowmajor ? (size_t)p * K + k : (size_t)k * npost + p;
-    syn[q] = syn_pack(pr.pre_idx[i], pr.delay[i]);
-    const float w = scaled_weight(pr.weight[i], t.scale_bits, bf16);
-    if (bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
+  // Each row sorted by (delay, pre, synapse): neighbouring entries then test
+  // bits of one history row at nearby words.  The pulled sum is an integer,
+  // so the order does not change it.
+  std::vector<size_t> start((size_t)npost + 1, 0);
+  for (size_t p = 0; p < (size_t)npost; ++p) start[p + 1] = start[p] + indeg[p];
+  std::vector<uint32_t> order(nnz);
+  {
+    std::vector<size_t> fill(start.begin(), start.end() - 1);
+    for (size_t i = 0; i < nnz; ++i) order[fill[pr.post_idx[i]]++] = (uint32_t)i;
   }
+  const auto key = [&](uint32_t i) {
+    return ((uint64_t)pr.delay[i] << 32) | (uint64_t)(uint32_t)pr.pre_idx[i];
+  };
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int32_t p = 0; p < npost; ++p)
+    std::sort(order.begin() + start[p], order.begin() + start[p + 1], [&](uint32_t x, uint32_t y) {
+      const uint64_t kx = key(x), ky = key(y);
+      return kx != ky ? kx < ky : x < y;
+    });
+  for (size_t p = 0; p < (size_t)npost; ++p) {
+    for (size_t j = start[p]; j < start[p + 1]; ++j) {
+      const uint32_t i = order[j];
+      const size_t k = j - start[p];
+      const size_t q = t.ell_rowmajor ? p * K + k : k * (size_t)npost + p;
+      syn[q] = ell_entry(pre_base + (uint32_t)pr.pre_idx[i], pr.delay[i], ell_shift);
+      const float w = scaled_weight(pr.weight[i], t.scale_bits, bf16);
+      if (bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
+    }
+  }
+  return true;
 }
 
 // Rebuilds the merged push table (every projection in CSR mode, cell-major)
@@ -182,26 +205,20 @@ static int upload_modes(Sim& s) {
                         (size_t)total * wsz, cudaMemcpyHostToDevice));
   }
   a.any_push = total > 0 ? 1u : 0u;
-  // Dense-pull work lists.
-  std::vector<PullTile> tiles;
-  std::vector<PullItem> items;
+  // Dense-pull work units.
+  std::vector<PullUnit> units;
   for (uint32_t pid = 0; pid < s.projs.size(); ++pid) {
     const ProjDev& P = s.projs[pid];
-    if (P.mode != SGB_PROP_ELL || P.ell_K == 0) continue;
-    if (!P.ell_rowmajor) {
-      for (uint32_t p0 = 0; p0 < P.post_count; p0 += 32) tiles.push_back({pid, p0});
-    } else {
-      for (uint32_t p = 0; p < P.post_count; ++p)
-        for (uint32_t k0 = 0; k0 < P.ell_K; k0 += kPullWarpChunk) items.push_back({pid, p, k0});
+    if (P.mode != SGB_PROP_ELL || P.ell_n == 0) continue;
+    for (uint32_t o = 0; o < P.ell_n; o += kPullUnit) {
+      units.push_back({pid, o});
+      if (P.ell_n - o <= kPullUnit) break;
     }
   }
-  if (!tiles.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.pull_tiles, tiles.data(), tiles.size() * sizeof(PullTile), cudaMemcpyHostToDevice));
-  if (!items.empty())
-    SGB_CUDA(cudaMemcpy((void*)a.pull_items, items.data(), items.size() * sizeof(PullItem), cudaMemcpyHostToDevice));
+  if (!units.empty())
+    SGB_CUDA(cudaMemcpy((void*)a.pull_units, units.data(), units.size() * sizeof(PullUnit), cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
-  a.n_pull_tiles = (uint32_t)tiles.size();
-  a.n_pull_items = (uint32_t)items.size();
+  a.n_pull_units = (uint32_t)units.size();
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
   return SGB_OK;
@@ -283,6 +300,10 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   if (s.segs.size() > 65535) return set_error(SGB_ERR_UNSUPPORTED, "more than 65535 segments");
   s.n_pad = (uint32_t)align_up(std::max<uint64_t>(cursor, 32), 32);
   s.n_words = s.n_pad / 32;
+  // Dense entries keep the cell index below bit ell_shift, with 2^(ell_shift
+  // - 10) >= the summary words per row (n_pad <= 2^27, so ell_shift <= 27).
+  s.ell_shift = 10;
+  while ((1ull << s.ell_shift) < s.n_pad) ++s.ell_shift;
   s.n_cells = first_id;
   s.ring_slots = (uint32_t)max_delay + 1;
   s.hist_rows = (uint32_t)max_delay;
@@ -334,11 +355,14 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       ell_syn.emplace_back();
       ell_wf.emplace_back();
       ell_wh.emplace_back();
-      build_ell(pr, net.pops[pr.post].num, s.bf16, t, ell_syn.back(), ell_wf.back(), ell_wh.back());
+      if (!build_ell(pr, net.pops[pr.post].num, s.segs[t.pre_seg].base, s.ell_shift,
+                     ell_pad(s.hist_rows, s.ell_shift), s.bf16, t, ell_syn.back(), ell_wf.back(),
+                     ell_wh.back()))
+        return set_error(SGB_ERR_UNSUPPORTED, "projection %zu: dense table over 2^32 entries", pj);
       t.off_ell_syn = pool;
       pool = align_up(pool + ell_syn.back().size() * 4, 256);
       t.off_ell_w = pool;
-      pool = align_up(pool + ell_syn.back().size() * wsz, 256);
+      pool = align_up(pool + (size_t)t.ell_K * net.pops[pr.post].num * wsz, 256);
       const SegDev& pre = s.segs[t.pre_seg];
       const SegDev& post = s.segs[t.post_seg];
       for (uint32_t p : pr.pre_idx) outdeg[pre.base + p]++;
@@ -354,6 +378,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       P.scale = ldexpf(1.0f, t.scale_bits);
       P.ell_K = t.ell_K;
       P.ell_rowmajor = t.ell_rowmajor ? 1u : 0u;
+      P.ell_n = t.ell_K * post.count;
       s.n_syn += t.nnz;
       s.projs.push_back(P);
       s.ptab.push_back(t);
@@ -368,12 +393,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       upd_words.push_back(w);
     }
   }
-  size_t cap_tiles = 0, cap_items = 0;
-  for (const ProjDev& P : s.projs) {
-    if (!P.ell_K) continue;
-    if (!P.ell_rowmajor) cap_tiles += (P.post_count + 31) / 32;
-    else cap_items += (size_t)P.post_count * ((P.ell_K + kPullWarpChunk - 1) / kPullWarpChunk);
-  }
+  size_t cap_units = 0;
+  for (const ProjDev& P : s.projs) cap_units += (P.ell_n + kPullUnit - 1) / kPullUnit;
 
   // ---- device memory ---------------------------------------------------------
   s.ell_bytes = std::max<size_t>(pool, 256);
@@ -384,7 +405,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     if (!ell_syn[i].empty()) {
       SGB_CUDA(cudaMemcpy(base + t.off_ell_syn, ell_syn[i].data(), ell_syn[i].size() * 4, cudaMemcpyHostToDevice));
       SGB_CUDA(cudaMemcpy(base + t.off_ell_w, s.bf16 ? (const void*)ell_wh[i].data() : (const void*)ell_wf[i].data(),
-                          ell_syn[i].size() * wsz, cudaMemcpyHostToDevice));
+                          (s.bf16 ? ell_wh[i].size() : ell_wf[i].size()) * wsz, cudaMemcpyHostToDevice));
     }
     s.projs[i].ell_syn = (const uint32_t*)(base + t.off_ell_syn);
     s.projs[i].ell_w = base + t.off_ell_w;
@@ -417,11 +438,14 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   const size_t o_mask = take((size_t)s.n_pad * 4);
   const size_t o_outdeg = take((size_t)s.n_pad * 4);
   const size_t o_words = take(std::max<size_t>(upd_words.size(), 1) * 4);
-  const size_t o_tiles = take(std::max<size_t>(cap_tiles, 1) * sizeof(PullTile));
-  const size_t o_items = take(std::max<size_t>(cap_items, 1) * sizeof(PullItem));
+  const size_t o_units = take(std::max<size_t>(cap_units, 1) * sizeof(PullUnit));
   const size_t o_state = take((size_t)s.n_pad * sizeof(float4));
   const size_t o_ring = take((size_t)s.ring_slots * s.n_pad * 8);
-  const size_t o_hist = take((size_t)s.hist_rows * s.n_words * 4);
+  // Spike history (two copies of H rows) followed by its summary (H + 1 rows
+  // of one bit per word): one region, cleared and snapshotted together.
+  const uint32_t n_swords = (s.n_words + 31) / 32;
+  s.hist_bytes = ((size_t)2 * s.hist_rows * s.n_words + (size_t)(s.hist_rows + 1) * n_swords) * 4;
+  const size_t o_hist = take(s.hist_bytes);
   const uint64_t item_cap = (uint64_t)s.n_pad + (uint64_t)(s.n_syn / kPushChunk) + 1;
   if (item_cap > 0xFFFFFFFFull) return set_error(SGB_ERR_UNSUPPORTED, "push work list too large");
   const size_t o_items_push = take((size_t)2 * item_cap * sizeof(uint2));
@@ -444,11 +468,15 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.src_mask = (const uint32_t*)(mb + o_mask);
   a.outdeg = (const uint32_t*)(mb + o_outdeg);
   a.upd_words = (const uint32_t*)(mb + o_words);
-  a.pull_tiles = (const PullTile*)(mb + o_tiles);
-  a.pull_items = (const PullItem*)(mb + o_items);
+  a.pull_units = (const PullUnit*)(mb + o_units);
   a.state = (float4*)(mb + o_state);
   a.ring = (int*)(mb + o_ring);
   a.hist = (uint32_t*)(mb + o_hist);
+  a.hsum = a.hist + (size_t)2 * s.hist_rows * s.n_words;
+  a.n_swords = n_swords;
+  a.ell_shift = s.ell_shift;
+  a.hist_rows = s.hist_rows;
+  a.pull_sum = pull_sum_bytes(a) <= kPullSumMax ? 1u : 0u;
   a.items = (uint2*)(mb + o_items_push);
   a.item_cap = (uint32_t)item_cap;
   a.counts = (uint32_t*)(mb + o_counts);
@@ -466,6 +494,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.bf16 = s.bf16 ? 1 : 0;
   a.substeps = cfg.substeps;
   s.deliver_blocks = 2 * s.sm_count;
+  SGB_CUDA(pull_setup());
+  s.pull_blocks = pull_blocks_per_sm(a) * s.sm_count;
   const int bpsm = std::min(cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : 1,
                             persistent_blocks_per_sm(s.bf16));
   s.persistent_blocks = std::max(1, bpsm) * s.sm_count;
@@ -512,7 +542,7 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
   const StepArgs& a = s.args;
   SGB_CUDA(cudaMemcpyAsync(a.state, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ring, 0, (size_t)s.ring_slots * s.n_pad * 8, s.stream));
-  SGB_CUDA(cudaMemsetAsync(a.hist, 0, (size_t)s.hist_rows * s.n_words * 4, s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.hist, 0, s.hist_bytes, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.items, 0, (size_t)2 * a.item_cap * sizeof(uint2), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.totals, 0, s.segs.size() * sizeof(double), s.stream));
@@ -537,6 +567,10 @@ static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nla
   } else {
     for (uint32_t i = 0; i < c; ++i) {
       if ((e = launch_update(a, st))) return e;
+      if (a.n_pull_units) {
+        if ((e = launch_pull(a, s.pull_blocks, st))) return e;
+        L++;
+      }
       if ((e = launch_deliver(a, s.deliver_blocks, st))) return e;
       L += 2;
     }
@@ -601,6 +635,7 @@ int sim_sync(Sim& s) {
   SGB_CUDA(cudaMemsetAsync(&s.args.ctl->error, 0, 4, s.stream));
   if (err & kErrBarrierTimeout)
     return set_error(SGB_ERR_DEVICE, "a device-side grid barrier hit its wait limit; reset the handle");
+
   return SGB_OK;
 }
 
@@ -663,6 +698,7 @@ int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int
   SGB_CUDA(cudaMemsetAsync(&s.args.ctl->error, 0, 4, s.stream));
   if (err & kErrBarrierTimeout)
     return set_error(SGB_ERR_DEVICE, "a device-side grid barrier hit its wait limit; reset the handle");
+
   if (overflow || (want_raster && (err & kErrRasterOverflow)))
     return set_error(SGB_ERR_OVERFLOW, "raster buffer too small; counts and state are intact");
   return SGB_OK;
@@ -848,7 +884,7 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   const StepArgs& a = s.args;
   const size_t b_state = (size_t)s.n_pad * sizeof(float4);
   const size_t b_ring = (size_t)s.ring_slots * s.n_pad * 8;
-  const size_t b_hist = (size_t)s.hist_rows * s.n_words * 4;
+  const size_t b_hist = s.hist_bytes;
   const size_t b_tot = s.segs.size() * sizeof(double);
   const size_t total = b_state + b_ring + b_hist + sizeof(Ctl) + b_tot;
   char* snap = nullptr;
@@ -935,15 +971,16 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
   const StepArgs& a = s.args;
   const double W = s.bf16 ? 2.0 : 4.0;
   // Algorithmic bytes: update = state 16 B read + 16 B write + ring 8 B per
-  // LIF cell, mask 4 B per input cell, 4 B per bitmap word, 8 B per push item
-  // written; deliver = per walked push synapse 4 B word + W weight + 8 B
-  // atomic, 8 B per push item read, per dense ELL entry 4 + W B plus 8 B per post.
-  double upd_bytes = (double)a.n_words * 4.0;
+  // LIF cell, mask 4 B per input cell, 8 B per bitmap word (two history
+  // copies), 8 B per push item written; deliver = per walked push synapse 4 B
+  // word + W weight + 8 B atomic, 8 B per push item read; pull = 4 B per
+  // stored dense entry plus, per entry whose pre cell spiked, W weight + 8 B
+  // atomic.
+  double upd_bytes = (double)a.n_words * 8.0;
   for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 40.0 * d.count : 4.0 * d.count;
-  double pull_bytes = 0;
+  double pull_entries = 0;
   for (const ProjDev& P : s.projs)
-    if (P.mode == SGB_PROP_ELL && P.ell_K)
-      pull_bytes += (double)P.post_count * P.ell_K * (4.0 + W) + (double)P.post_count * 8.0;
+    if (P.mode == SGB_PROP_ELL) pull_entries += (double)P.ell_n;
   cudaEvent_t ev[2 * K];
   for (auto& e : ev) SGB_CUDA(cudaEventCreate(&e));
   double tot_ms[K] = {0}, tot_bytes[K] = {0};
@@ -959,6 +996,9 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
       SGB_CUDA(cudaEventRecord(ev[0], s.stream));
       SGB_CUDA(launch_update(a, s.stream));
       SGB_CUDA(cudaEventRecord(ev[1], s.stream));
+      SGB_CUDA(cudaEventRecord(ev[4], s.stream));
+      SGB_CUDA(launch_pull(a, s.pull_blocks, s.stream));
+      SGB_CUDA(cudaEventRecord(ev[5], s.stream));
       SGB_CUDA(cudaEventRecord(ev[2], s.stream));
       SGB_CUDA(launch_deliver(a, s.deliver_blocks, s.stream));
       SGB_CUDA(cudaEventRecord(ev[3], s.stream));
@@ -966,9 +1006,11 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
       SGB_CUDA(cudaStreamSynchronize(s.stream));
       const double items = (double)after.active_count[before.step & 1];
       const double walked = (double)(after.delivered - before.delivered);
-      const double step_bytes[K] = {upd_bytes + items * 8.0,
-                                    walked * (12.0 + W) + items * 8.0 + pull_bytes};
+      const double pulled = (double)(after.pulled - before.pulled);
+      const double step_bytes[K] = {upd_bytes + items * 8.0, walked * (12.0 + W) + items * 8.0,
+                                    pull_entries * 4.0 + pulled * (8.0 + W)};
       for (int k = 0; k < K; ++k) {
+        if (k == 2 && !a.n_pull_units) continue;
         float ms = 0.f;
         SGB_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
         tot_ms[k] += ms;

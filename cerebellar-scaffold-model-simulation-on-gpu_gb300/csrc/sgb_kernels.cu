@@ -36,6 +36,7 @@ struct StepIdx {
   unsigned long long t;
   uint32_t slot;  // t % ring_slots
   uint32_t hrow;  // t % hist_rows
+  uint32_t srow;  // t % (hist_rows + 1): spike-summary row
   uint32_t rel;   // step index within the chunk
 };
 
@@ -133,6 +134,25 @@ __device__ __forceinline__ uint32_t item_tag(unsigned long long t) {
   return ((uint32_t)t & 0x3FFFFFu) | 0x400000u;  // never 0 (cleared)
 }
 
+// Spike bits of word w at step t: both copies of the history row, and, when
+// any cell of the word spiked, the word's bit in the step's summary row.
+__device__ __forceinline__ void put_hist(const StepArgs& a, const StepIdx& ix, uint32_t w,
+                                         uint32_t bits) {
+  __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, bits);
+  __stcg(a.hist + (size_t)(ix.hrow + a.hist_rows) * a.n_words + w, bits);
+  if (bits) atomicOr(a.hsum + (size_t)ix.srow * a.n_swords + (w >> 5), 1u << (w & 31u));
+}
+
+// The summary row of step t + 1 is free during step t (the oldest row a pull
+// of step t reads is that of t + 1 - H); threads gtid, gtid + gthreads, ...
+// clear it.
+__device__ __forceinline__ void clear_next_summary(const StepArgs& a, const StepIdx& ix,
+                                                   uint32_t gtid, uint32_t gthreads) {
+  const uint32_t row = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
+  for (uint32_t j = gtid; j < a.n_swords; j += gthreads)
+    __stcg(a.hsum + (size_t)row * a.n_swords + j, 0u);
+}
+
 // One cell's step; state and constants in registers, ring slot consumed.
 __device__ __forceinline__ bool cell_fire(const StepArgs& a, const SegDev& sd, uint32_t i,
                                           uint32_t local, bool valid, float4& st, uint32_t mask,
@@ -153,7 +173,7 @@ __device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint
                                              uint32_t outdeg, const StepIdx& ix) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ballot = __ballot_sync(kFull, fired);
-  if (lane == 0) __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, ballot);
+  if (lane == 0) put_hist(a, ix, w, ballot);
   if (ballot == 0) return;
   const uint32_t n = __popc(ballot);
   const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
@@ -295,63 +315,61 @@ __device__ __forceinline__ uint32_t push_item(const StepArgs& a, uint2 it, uint3
   return it.y >> 23;
 }
 
-__device__ __forceinline__ uint32_t spike_bit(const StepArgs& a, uint32_t hrow,
-                                              uint32_t pre_global, uint32_t d) {
-  uint32_t row = hrow + 1u + a.hist_rows - d;  // row of step t + 1 - d
-  if (row >= a.hist_rows) row -= a.hist_rows;
-  if (row >= a.hist_rows) row -= a.hist_rows;
-  return (__ldcg(a.hist + (size_t)row * a.n_words + (pre_global >> 5)) >> (pre_global & 31u)) & 1u;
+// ---- dense pull (ELL) ----------------------------------------------------------
+// A unit is kPullUnit consecutive entries of one projection's ELL, whatever
+// its layout.  An entry names its pre cell and delay, so its spike bit of
+// step t + 1 - d is one load from the doubled history (row hrow + H + 1 - d,
+// no wrap); for the few entries whose pre cell spiked the weight is read and
+// added into the post cell's ring slot with one atomic (the post is
+// recovered from the entry's offset).
+__device__ __forceinline__ const uint32_t* hist_word(const StepArgs& a, uint32_t hrow, uint32_t e) {
+  const uint32_t d1 = e >> a.ell_shift;  // delay - 1
+  const uint32_t g = e & ((1u << a.ell_shift) - 1u);
+  return a.hist + (size_t)(hrow + a.hist_rows - d1) * a.n_words + (g >> 5);
 }
 
-// Column-major ELL: each lane owns one post cell; column k of all posts is
-// contiguous, so the warp reads consecutive words per k.
 template <bool BF16>
-__device__ __forceinline__ void pull_tile(const StepArgs& a, const PullTile& tile,
-                                          const StepIdx& ix) {
-  const ProjDev& P = a.projs[tile.proj];
-  const uint32_t p = tile.post_start + (threadIdx.x & 31u);
-  if (p >= P.post_count) return;
-  int acc = 0;
-  for (uint32_t k = 0; k < P.ell_K; ++k) {
-    const uint32_t q = k * P.post_count + p;
-    const uint32_t wd = __ldg(P.ell_syn + q);
-    if (wd == kEllPad) break;  // padding is at the end of each row
-    if (spike_bit(a, ix.hrow, P.pre_base + (wd & kIndexMask), wd >> kIndexBits))
-      acc += __float2int_rn(load_weight<BF16>(P.ell_w, q));
-  }
-  if (acc) {
-    uint32_t slot = ix.slot + 1u;
-    if (slot >= a.ring_slots) slot -= a.ring_slots;
-    atomicAdd(a.ring + (((size_t)slot * a.n_pad + P.post_base + p) << 1) + P.channel, acc);
-  }
+__device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, uint32_t o,
+                                         uint32_t slot1) {
+  const uint32_t post = P.ell_rowmajor ? o / P.ell_K : o % P.post_count;
+  const int v = __float2int_rn(load_weight<BF16>(P.ell_w, o));
+  atomicAdd(a.ring + (((size_t)slot1 * a.n_pad + P.post_base + post) << 1) + P.channel, v);
 }
 
-// Row-major ELL for wide rows: the warp strides over one row chunk.
+// Persistent kernels: entries straight from global memory, 8 per lane per
+// batch (their 64-register budget), history from L2 (other blocks write it
+// during the launch).  Returns the lane's hits.
 template <bool BF16>
-__device__ __forceinline__ void pull_item(const StepArgs& a, const PullItem& it,
-                                          const StepIdx& ix) {
-  const ProjDev& P = a.projs[it.proj];
+__device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit un,
+                                              uint32_t hrow, uint32_t slot1) {
+  constexpr uint32_t B = 8;
+  const ProjDev& P = a.projs[un.proj];
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t k1 = min(it.k0 + (uint32_t)kPullWarpChunk, P.ell_K);
-  const size_t row = (size_t)it.post * P.ell_K;
-  int acc = 0;
-  for (uint32_t k = it.k0 + lane; k < k1; k += 32) {
-    const uint32_t wd = __ldg(P.ell_syn + row + k);
-    if (wd != kEllPad && spike_bit(a, ix.hrow, P.pre_base + (wd & kIndexMask), wd >> kIndexBits))
-      acc += __float2int_rn(load_weight<BF16>(P.ell_w, (uint32_t)(row + k)));
+  uint32_t hits = 0;
+#pragma unroll 1
+  for (uint32_t ob = un.o0 + lane; ob < un.o0 + kPullUnit; ob += 32u * B) {
+    uint32_t e[B];
+#pragma unroll
+    for (uint32_t u = 0; u < B; ++u) e[u] = __ldg(P.ell_syn + ob + 32u * u);  // padded to units
+    uint32_t hit = 0;
+#pragma unroll
+    for (uint32_t u = 0; u < B; ++u)
+      if ((e[u] >> a.ell_shift) < a.hist_rows)
+        hit |= ((__ldcg(hist_word(a, hrow, e[u])) >> (e[u] & 31u)) & 1u) << u;
+    hits += __popc(hit);
+    while (hit) {
+      const uint32_t u = __ffs(hit) - 1;
+      hit &= hit - 1;
+      pull_hit<BF16>(a, P, ob + 32u * u, slot1);
+    }
   }
-  acc = __reduce_add_sync(kFull, acc);
-  if (lane == 0 && acc) {
-    uint32_t slot = ix.slot + 1u;
-    if (slot >= a.ring_slots) slot -= a.ring_slots;
-    atomicAdd(a.ring + (((size_t)slot * a.n_pad + P.post_base + it.post) << 1) + P.channel, acc);
-  }
+  return hits;
 }
 
 // Delivery phase for one warp: push items gw, gw + nw, ... up to the first
 // slot not written this step (each delivered item is cleared), then the dense
 // pull units.  Returns the synapses walked by the push items.
-template <bool BF16>
+template <bool BF16, bool PULL>
 __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw, uint32_t nw,
                                                  const StepIdx& ix) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -366,21 +384,23 @@ __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw,
       walked += push_item<BF16>(a, it, ix.slot);
     }
   }
-  const uint32_t n_pull = a.n_pull_tiles + a.n_pull_items;
-  for (uint32_t u = gw; u < n_pull; u += nw) {
-    if (u < a.n_pull_tiles)
-      pull_tile<BF16>(a, a.pull_tiles[u], ix);
-    else
-      pull_item<BF16>(a, a.pull_items[u - a.n_pull_tiles], ix);
+  if (PULL && a.n_pull_units) {
+    const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+    uint32_t hits = 0;
+    for (uint32_t u = gw; u < a.n_pull_units; u += nw) hits += pull_unit<BF16>(a, a.pull_units[u], ix.hrow, slot1);
+    hits = __reduce_add_sync(kFull, hits);
+    if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
   }
   return walked;
 }
 
-__device__ __forceinline__ StepIdx step_of(const Ctl* ctl) {
+__device__ __forceinline__ StepIdx step_of(const StepArgs& a) {
+  const Ctl* ctl = a.ctl;
   StepIdx ix;
   ix.t = ctl->step;
   ix.slot = ctl->ring_slot;
   ix.hrow = ctl->hist_row;
+  ix.srow = (uint32_t)(ix.t % (a.hist_rows + 1ull));
   ix.rel = ctl->t_rel;
   return ix;
 }
@@ -393,9 +413,11 @@ __global__ void k_chunk_begin(StepArgs a) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_update(StepArgs a) {
-  const uint32_t w = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const uint32_t gtid = blockIdx.x * kBlock + threadIdx.x;
+  const uint32_t w = gtid >> 5;
+  const StepIdx ix = step_of(a);
+  clear_next_summary(a, ix, gtid, gridDim.x * kBlock);
   if (w >= a.n_words) return;
-  const StepIdx ix = step_of(a.ctl);
   update_word(a, w, ix);
 }
 
@@ -404,9 +426,9 @@ __global__ void __launch_bounds__(kBlock) k_update(StepArgs a) {
 template <bool BF16>
 __global__ void __launch_bounds__(kBlock) k_deliver(StepArgs a) {
   Ctl* ctl = a.ctl;
-  const StepIdx ix = step_of(ctl);
+  const StepIdx ix = step_of(a);
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t walked = deliver_warp<BF16>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5,
+  const uint32_t walked = deliver_warp<BF16, false>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5,
                                              (gridDim.x * kBlock) >> 5, ix);
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   // Step bookkeeping by the last block to arrive.
@@ -427,6 +449,94 @@ __global__ void __launch_bounds__(kBlock) k_deliver(StepArgs a) {
     ctl->t_rel = ix.rel + 1u;
     a.raster_off[ix.rel + 1u] = ctl->raster_count;
   }
+}
+
+// Dense pull of the per-step driver (one 1,024-thread block per SM).  Each
+// block stages the summary rows of steps t + 1 - d, d = 1..H (one bit per
+// 32-cell word: did any cell of it spike) in shared memory, delay-major with
+// a power-of-two stride so an entry's summary word is s_sum[e >> 10]; row H
+// stays zero, so padding entries (delay field H) never pass.  Warps stream
+// units (gw, gw + nw, ...; the first one's loads overlap the staging): a lane
+// loads its 32 entries of a unit at once, settles every entry whose summary
+// bit is clear in shared memory, and walks the few that passed four at a
+// time (usually one trip per warp), loading each entry again (an L1 hit) and
+// then its history word (through L1: the history is read-only in this
+// launch).  Without room for the summary (SUM false) every entry walks.
+template <bool BF16, bool SUM>
+__global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
+  constexpr uint32_t E = kPullUnit / 32;  // entries per lane per unit
+  constexpr uint32_t W = 4;               // entries walked per trip
+  extern __shared__ uint32_t s_sum[];     // [H + 1][2^(ell_shift - 10)]
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
+  const uint32_t n = a.n_pull_units;
+  const StepIdx ix = step_of(a);
+  const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+  uint32_t e[E];
+  if (gw < n) {
+    const PullUnit un = a.pull_units[gw];
+    const uint32_t* src = a.projs[un.proj].ell_syn + un.o0 + lane;
+#pragma unroll
+    for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
+  }
+  if (SUM) {
+    const uint32_t R = a.hist_rows + 1u, stride_log = a.ell_shift - 10u;
+    for (uint32_t d1 = 0; d1 < a.hist_rows; ++d1) {
+      const uint32_t src = (ix.srow + R - d1) % R;  // row of step t - d1
+      for (uint32_t j = threadIdx.x; j < a.n_swords; j += kPullBlock)
+        s_sum[(d1 << stride_log) + j] = __ldg(a.hsum + (size_t)src * a.n_swords + j);
+    }
+    if (threadIdx.x == 0) s_sum[a.hist_rows << stride_log] = 0u;  // padding's word
+    __syncthreads();
+  }
+  // History word of entry e: row hrow + H - (delay - 1) of the doubled history.
+  const uint32_t* hist_top = a.hist + (size_t)(ix.hrow + a.hist_rows) * a.n_words;
+  const uint32_t gmask = (1u << a.ell_shift) - 1u;
+  uint32_t hits = 0;
+  for (uint32_t u = gw; u < n; u += nw) {
+    const PullUnit un = a.pull_units[u];
+    const ProjDev& P = a.projs[un.proj];
+    const uint32_t* src = P.ell_syn + un.o0 + lane;  // tables are padded to whole units
+    if (u != gw) {
+#pragma unroll
+      for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
+    }
+    uint32_t need = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < E; ++k) {
+      if (SUM) {
+        const uint32_t sw = s_sum[e[k] >> 10];
+        need |= (__funnelshift_r(sw, sw, e[k] >> 5) & 1u) << k;
+      } else {
+        need |= (uint32_t)((e[k] >> a.ell_shift) < a.hist_rows) << k;
+      }
+    }
+    while (need) {
+      uint32_t ks[W], ev[W], hw[W];
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) {
+        ks[j] = need ? __ffs(need) - 1u : E;
+        need &= need - 1u;
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) ev[j] = ks[j] < E ? __ldg(src + ks[j] * 32u) : 0u;
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j)
+        hw[j] = ks[j] < E ? __ldg(hist_top - (size_t)(ev[j] >> a.ell_shift) * a.n_words +
+                                  ((ev[j] & gmask) >> 5))
+                          : 0u;
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) {
+        if (ks[j] < E && ((hw[j] >> (ev[j] & 31u)) & 1u)) {
+          ++hits;
+          pull_hit<BF16>(a, P, un.o0 + ks[j] * 32u + lane, slot1);
+        }
+      }
+    }
+  }
+  hits = __reduce_add_sync(kFull, hits);
+  if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
 }
 
 // Per-segment spike totals of the chunk, folded into the FP64 accumulators.
@@ -485,7 +595,7 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
 template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
   Ctl* ctl = a.ctl;
-  StepIdx ix = step_of(ctl);
+  StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
@@ -498,13 +608,15 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     ix.rel = s;
     // Item counter of step t + 1: its last user was the update of step t - 1.
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
+    clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     update_words(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
-    if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
-    walked += deliver_warp<BF16>(a, gw, nw, ix);
+    if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
+    walked += deliver_warp<BF16, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
     ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+    ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
@@ -523,7 +635,7 @@ template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepArgs a,
                                                                           uint32_t n_steps) {
   Ctl* ctl = a.ctl;
-  StepIdx ix = step_of(ctl);
+  StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
@@ -556,16 +668,18 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     ix.t = t0 + s;
     ix.rel = s;
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
+    clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     if (has) {
       const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
       publish_word(a, w, seg, i, fired, r0, r1, od, ix);
     }
     if (!grid_barrier(a, target)) break;
-    if (leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
-    walked += deliver_warp<BF16>(a, gw, nw, ix);
+    if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
+    walked += deliver_warp<BF16, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) break;
     ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+    ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
   if (valid && lif) a.state[i] = st;
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
@@ -590,9 +704,9 @@ template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs a,
                                                                        uint32_t n_steps) {
   __shared__ uint2 s_items[kBlockItems];
-  __shared__ uint32_t s_n;
+  __shared__ uint32_t s_n[2];  // item count of step parity p; the other one is reset
   Ctl* ctl = a.ctl;
-  StepIdx ix = step_of(ctl);
+  StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t wib = threadIdx.x >> 5;
@@ -619,18 +733,19 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   }
   unsigned long long target = 0;
   uint32_t walked = 0;
-  uint32_t s = 0;
-  for (; s < n_steps; ++s) {
+  if (threadIdx.x == 0) s_n[0] = s_n[1] = 0;
+  __syncthreads();
+  for (uint32_t s = 0; s < n_steps; ++s) {
     ix.t = t0 + s;
     ix.rel = s;
-    if (threadIdx.x == 0) s_n = 0;
-    if (leader && s > 0) a.raster_off[s] = __ldcg(&ctl->raster_count);
-    __syncthreads();
+    const uint32_t par = s & 1u;
+    if (a.raster_cap && leader && s > 0) a.raster_off[s] = __ldcg(&ctl->raster_count);
+    clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     uint32_t off = 0, nit = 0;
     if (has) {
       const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
       const uint32_t ballot = __ballot_sync(kFull, fired);
-      if (lane == 0) __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, ballot);
+      if (lane == 0) put_hist(a, ix, w, ballot);
       if (ballot) {
         const uint32_t n = __popc(ballot);
         const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
@@ -645,7 +760,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         const uint32_t tot = __shfl_sync(kFull, incl, 31);
         uint32_t roff = 0;
         if (lane == 0) {
-          if (tot) off = atomicAdd(&s_n, tot);
+          if (tot) off = atomicAdd(&s_n[par], tot);
           atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], n);
           if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
           if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
@@ -667,7 +782,9 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       }
     }
     __syncthreads();
-    const uint32_t n_items = min(s_n, kBlockItems);
+    const uint32_t n_items = min(s_n[par], kBlockItems);
+    // The other parity's count was last read before this step's __syncthreads.
+    if (threadIdx.x == 0) s_n[par ^ 1u] = 0;
     for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32)
       walked += push_item<BF16>(a, s_items[u], ix.slot);
     // Items beyond the block's capacity are delivered by the warp that made them.
@@ -685,12 +802,13 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     if (!grid_barrier(a, target)) break;
     ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+    ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
   if (valid && lif) a.state[i] = st;
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
-    a.raster_off[n_steps] = __ldcg(&ctl->raster_count);
+    if (a.raster_cap) a.raster_off[n_steps] = __ldcg(&ctl->raster_count);
     ctl->step = t0 + n_steps;
     ctl->ring_slot = ix.slot;
     ctl->hist_row = ix.hrow;
@@ -719,6 +837,40 @@ cudaError_t launch_deliver(const StepArgs& a, int blocks, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+size_t pull_sum_bytes(const StepArgs& a) {
+  return (size_t)(a.hist_rows + 1u) << (a.ell_shift - 10u + 2u);
+}
+
+static size_t pull_smem_bytes(const StepArgs& a) { return a.pull_sum ? pull_sum_bytes(a) : 0; }
+
+cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
+  if (!a.n_pull_units) return cudaSuccess;
+  const size_t smem = pull_smem_bytes(a);
+  if (a.bf16) {
+    if (a.pull_sum) k_pull<true, true><<<blocks, kPullBlock, smem, s>>>(a);
+    else k_pull<true, false><<<blocks, kPullBlock, smem, s>>>(a);
+  } else {
+    if (a.pull_sum) k_pull<false, true><<<blocks, kPullBlock, smem, s>>>(a);
+    else k_pull<false, false><<<blocks, kPullBlock, smem, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t pull_setup() {
+  const int mx = (int)kPullSumMax;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_pull<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_pull<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_pull<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  return cudaFuncSetAttribute(k_pull<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+int pull_blocks_per_sm(const StepArgs& a) {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_pull<true, true>, kPullBlock, pull_smem_bytes(a));
+  return n > 0 ? n : 1;
+}
+
 cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
   if (!a.n_segs) return cudaSuccess;
   k_chunk_end<<<a.n_segs, kBlock, 0, s>>>(a);
@@ -744,7 +896,15 @@ int persistent_blocks_per_sm(bool bf16) {
 int persistent_kernel_kind(const StepArgs& a, int blocks) {
   const bool resident = (uint64_t)a.n_upd_words * 32u <= (uint64_t)blocks * kPersistBlock;
   if (!resident) return SGB_KERNEL_GENERAL;
-  return a.n_pull_tiles == 0 && a.n_pull_items == 0 ? SGB_KERNEL_FUSED : SGB_KERNEL_RESIDENT;
+  return a.n_pull_units == 0 ? SGB_KERNEL_FUSED : SGB_KERNEL_RESIDENT;
+}
+
+// Register-resident kernels need one warp per word and no more: fewer blocks
+// mean fewer arrivals at every grid barrier.
+static int persistent_grid(const StepArgs& a, int blocks, int kind) {
+  if (kind == SGB_KERNEL_GENERAL) return blocks;
+  const int need = (int)((a.n_upd_words + kPersistBlock / 32 - 1) / (kPersistBlock / 32));
+  return need < 1 ? 1 : (need < blocks ? need : blocks);
 }
 
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s) {
@@ -760,7 +920,8 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                                         : (const void*)k_persistent_resident<false>)
                               : (a.bf16 ? (const void*)k_persistent<true>
                                         : (const void*)k_persistent<false>);
-  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, 0, s);
+  return cudaLaunchCooperativeKernel(fn, dim3(persistent_grid(a, blocks, kind)), dim3(kPersistBlock),
+                                     params, 0, s);
 }
 
 }  // namespace sgb

@@ -100,15 +100,21 @@ SGB_HD float bf16_bits_to_f32(uint16_t h) {
   return v.f;
 }
 
-// Synapse word packing.  Low 28 bits: population-local neuron index (pre for
-// the post-major ELL table, post for the pre-major CSR table); high 4 bits:
-// the delay in exchange steps (1..15).  The ELL pad entry is all ones.
+// Population sizes are bounded by the 28-bit index space; delays are 1..15
+// exchange steps.
 constexpr uint32_t kIndexBits = 28;
 constexpr uint32_t kIndexMask = (1u << kIndexBits) - 1u;
-constexpr uint32_t kEllPad = 0xFFFFFFFFu;
 constexpr int kMaxDelay = 15;
-SGB_HD uint32_t syn_pack(uint32_t index, uint32_t delay) {
-  return (index & kIndexMask) | (delay << kIndexBits);
+
+// Dense-pull (ELL) entry: the pre cell's global (padded) index g in the low
+// `shift` bits and delay - 1 above them, so the entry names the spike bit of
+// step t + 1 - d directly.  shift = 10 + log2 of the spike-summary row stride
+// (a power of two >= the summary words per row), which makes e >> 10 the
+// entry's summary word and (e >> 5) & 31 its bit there.  Padding carries the
+// delay field H (one past the deepest delay): ell_pad(H, shift).
+SGB_HD uint32_t ell_entry(uint32_t g, uint32_t delay, uint32_t shift) {
+  return ((delay - 1u) << shift) | g;
 }
+SGB_HD uint32_t ell_pad(uint32_t hist_rows, uint32_t shift) { return hist_rows << shift; }
 
 }  // namespace sgb

@@ -22,7 +22,7 @@ PROP_AUTO, PROP_CSR, PROP_ELL = 0, 1, 2
 WEIGHT_FP32, WEIGHT_BF16 = 0, 1
 EXEC_GRAPH, EXEC_PERSISTENT, EXEC_STREAM = 0, 1, 2
 INPUT_POISSON, INPUT_PERIODIC = 0, 1
-KCLASS_COUNT = 2
+KCLASS_COUNT = 3
 KERNEL_NAMES = {0: "k_update+k_deliver", 1: "k_persistent", 2: "k_persistent_resident",
                 3: "k_persistent_fused"}
 
@@ -76,7 +76,8 @@ class SimInfo(C.Structure):
                 ("step", C.c_int64), ("device_bytes", C.c_int64), ("exec_mode", C.c_int32),
                 ("weight_type", C.c_int32), ("substeps", C.c_int32), ("chunk_steps", C.c_int32),
                 ("dt_ms", C.c_double), ("events", C.c_int64), ("delivered", C.c_int64),
-                ("step_kernel", C.c_int32), ("reserved_", C.c_int32)]
+                ("step_kernel", C.c_int32), ("reserved_", C.c_int32), ("pulled", C.c_int64),
+                ("pull_entries", C.c_int64)]
 
 
 P = C.POINTER

@@ -135,6 +135,8 @@ typedef struct sgb_sim_info {
   int64_t delivered;     /* synapses walked by event-driven delivery since the last reset */
   int32_t step_kernel;   /* SGB_KERNEL_*: the kernel a chunk of steps runs in            */
   int32_t reserved_;
+  int64_t pulled;        /* dense-pull entries whose pre cell had spiked (deliveries) since the last reset */
+  int64_t pull_entries;  /* dense-table entries streamed per step (0 without dense projections) */
 } sgb_sim_info;
 
 /* Step kernels (sgb_sim_info.step_kernel). */
@@ -317,10 +319,11 @@ int sgb_sim_launch_count(const sgb_sim* sim, int64_t* launches);
 
 /* Instrumented run: advances n_steps with the per-step kernels launched one by
  * one, each bracketed by CUDA events on the handle's stream, and returns per
- * kernel class (0 update, 1 deliver) the mean device time per launch in
- * microseconds, the mean algorithmic bytes per launch, and the number of
- * launches. */
-#define SGB_KCLASS_COUNT 2
+ * kernel class (0 update, 1 event-driven delivery, 2 dense pull) the mean
+ * device time per launch in microseconds, the mean algorithmic bytes per
+ * launch, and the number of launches (0 for the pull without dense
+ * projections). */
+#define SGB_KCLASS_COUNT 3
 int sgb_sim_profile(sgb_sim* sim, int32_t n_steps, double* mean_us, double* bytes_per_launch,
                     int64_t* launches);
 
