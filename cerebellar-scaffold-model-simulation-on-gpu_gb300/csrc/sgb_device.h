@@ -32,7 +32,7 @@ constexpr int kPersistBlock = 1024;   // threads per block of the persistent ker
 constexpr uint32_t kPushChunk = 256;  // synapses per push work item (8 per lane)
 constexpr uint32_t kPullUnit = 1024;  // ELL entries per dense-pull work unit (32 per lane)
 constexpr int kPullBlock = 1024;             // threads per k_pull block (one per SM)
-constexpr size_t kPullSumMax = 192 * 1024;  // largest spike summary k_pull stages (H + 1 rows)
+constexpr size_t kPullSumMax = 192 * 1024;  // largest spike summary k_pull stages (H rows)
 constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-major layout
 // Push-table synapse word: 27-bit padded post index, 4-bit delay, 1-bit accumulator.
 constexpr uint32_t kPushPostBits = 27;
@@ -122,7 +122,7 @@ struct StepArgs {
   const PullUnit* pull_units;
   float4* state;
   int* ring;                      // int2 per cell per slot, viewed as int[2]
-  uint32_t* hist;                 // [2H][n_words]: row r and r + H hold step r mod H
+  uint32_t* hist;                 // [2H][n_words]: rows H-1-(t mod H) and 2H-1-(t mod H) hold step t
   uint32_t* hsum;                 // [H + 1][n_swords]: bit w of row t mod (H + 1) = word w
                                   // of step t had a spike
   uint2* items;                   // [2][item_cap] push work ranges
@@ -135,7 +135,6 @@ struct StepArgs {
   uint32_t ring_slots, hist_rows;
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
-  uint32_t ell_shift;             // ELL entry = (delay - 1) << ell_shift | cell
   uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory
   uint32_t any_push;
   uint32_t raster_cap;

@@ -114,7 +114,7 @@ static float scaled_weight(float w, int32_t bits, bool bf16) {
 // of each row; column-major for narrow rows, row-major for wide ones (either
 // way the pull streams it as flat units, so the table is padded to whole
 // units).  Entries are ell_entry words (at most 2^27 padded cells).
-static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, uint32_t ell_shift,
+static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, uint32_t n_pad,
                       uint32_t pad, bool bf16, ProjTables& t, std::vector<uint32_t>& syn,
                       std::vector<float>& wf, std::vector<uint16_t>& wh) {
   const size_t nnz = pr.pre_idx.size();
@@ -152,7 +152,7 @@ static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, ui
       const uint32_t i = order[j];
       const size_t k = j - start[p];
       const size_t q = t.ell_rowmajor ? p * K + k : k * (size_t)npost + p;
-      syn[q] = ell_entry(pre_base + (uint32_t)pr.pre_idx[i], pr.delay[i], ell_shift);
+      syn[q] = ell_entry(pre_base + (uint32_t)pr.pre_idx[i], pr.delay[i], n_pad);
       const float w = scaled_weight(pr.weight[i], t.scale_bits, bf16);
       if (bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
     }
@@ -298,12 +298,12 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       for (uint8_t d : pr.delay) max_delay = std::max(max_delay, (int)d);
   }
   if (s.segs.size() > 65535) return set_error(SGB_ERR_UNSUPPORTED, "more than 65535 segments");
-  s.n_pad = (uint32_t)align_up(std::max<uint64_t>(cursor, 32), 32);
+  // A multiple of 1,024 cells, so dense entries (delay - 1) * n_pad + g keep
+  // the word and summary-word structure of g (see ell_entry).
+  s.n_pad = (uint32_t)align_up(std::max<uint64_t>(cursor, 1024), 1024);
+  if (s.n_pad > kPushPostMask + 1u)
+    return set_error(SGB_ERR_UNSUPPORTED, "more than 2^27 cells (with padding) in one handle");
   s.n_words = s.n_pad / 32;
-  // Dense entries keep the cell index below bit ell_shift, with 2^(ell_shift
-  // - 10) >= the summary words per row (n_pad <= 2^27, so ell_shift <= 27).
-  s.ell_shift = 10;
-  while ((1ull << s.ell_shift) < s.n_pad) ++s.ell_shift;
   s.n_cells = first_id;
   s.ring_slots = (uint32_t)max_delay + 1;
   s.hist_rows = (uint32_t)max_delay;
@@ -355,8 +355,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       ell_syn.emplace_back();
       ell_wf.emplace_back();
       ell_wh.emplace_back();
-      if (!build_ell(pr, net.pops[pr.post].num, s.segs[t.pre_seg].base, s.ell_shift,
-                     ell_pad(s.hist_rows, s.ell_shift), s.bf16, t, ell_syn.back(), ell_wf.back(),
+      if (!build_ell(pr, net.pops[pr.post].num, s.segs[t.pre_seg].base, s.n_pad,
+                     ell_pad(s.hist_rows, s.n_pad), s.bf16, t, ell_syn.back(), ell_wf.back(),
                      ell_wh.back()))
         return set_error(SGB_ERR_UNSUPPORTED, "projection %zu: dense table over 2^32 entries", pj);
       t.off_ell_syn = pool;
@@ -474,7 +474,6 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.hist = (uint32_t*)(mb + o_hist);
   a.hsum = a.hist + (size_t)2 * s.hist_rows * s.n_words;
   a.n_swords = n_swords;
-  a.ell_shift = s.ell_shift;
   a.hist_rows = s.hist_rows;
   a.pull_sum = pull_sum_bytes(a) <= kPullSumMax ? 1u : 0u;
   a.items = (uint2*)(mb + o_items_push);

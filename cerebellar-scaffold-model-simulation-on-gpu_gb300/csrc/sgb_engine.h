@@ -54,7 +54,6 @@ struct Sim {
   int deliver_blocks = 0;
   int pull_blocks = 0;        // k_pull grid (resident blocks per SM x SMs)
   size_t hist_bytes = 0;      // spike history + its summary
-  uint32_t ell_shift = 10;    // dense-entry delay field position
   int persistent_blocks = 0;
   SrcDev* h_srcs = nullptr;  // pinned staging of the source table
 

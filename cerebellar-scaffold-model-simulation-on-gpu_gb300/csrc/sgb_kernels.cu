@@ -138,8 +138,9 @@ __device__ __forceinline__ uint32_t item_tag(unsigned long long t) {
 // any cell of the word spiked, the word's bit in the step's summary row.
 __device__ __forceinline__ void put_hist(const StepArgs& a, const StepIdx& ix, uint32_t w,
                                          uint32_t bits) {
-  __stcg(a.hist + (size_t)ix.hrow * a.n_words + w, bits);
-  __stcg(a.hist + (size_t)(ix.hrow + a.hist_rows) * a.n_words + w, bits);
+  const uint32_t r = a.hist_rows - 1u - ix.hrow;  // rows in decreasing step order
+  __stcg(a.hist + (size_t)r * a.n_words + w, bits);
+  __stcg(a.hist + (size_t)(r + a.hist_rows) * a.n_words + w, bits);
   if (bits) atomicOr(a.hsum + (size_t)ix.srow * a.n_swords + (w >> 5), 1u << (w & 31u));
 }
 
@@ -317,15 +318,12 @@ __device__ __forceinline__ uint32_t push_item(const StepArgs& a, uint2 it, uint3
 
 // ---- dense pull (ELL) ----------------------------------------------------------
 // A unit is kPullUnit consecutive entries of one projection's ELL, whatever
-// its layout.  An entry names its pre cell and delay, so its spike bit of
-// step t + 1 - d is one load from the doubled history (row hrow + H + 1 - d,
-// no wrap); for the few entries whose pre cell spiked the weight is read and
-// added into the post cell's ring slot with one atomic (the post is
-// recovered from the entry's offset).
-__device__ __forceinline__ const uint32_t* hist_word(const StepArgs& a, uint32_t hrow, uint32_t e) {
-  const uint32_t d1 = e >> a.ell_shift;  // delay - 1
-  const uint32_t g = e & ((1u << a.ell_shift) - 1u);
-  return a.hist + (size_t)(hrow + a.hist_rows - d1) * a.n_words + (g >> 5);
+// its layout.  An entry is the offset of its spike bit above the step's
+// history base (word e >> 5, bit e & 31); for the few entries whose pre cell
+// spiked the weight is read and added into the post cell's ring slot with one
+// atomic (the post is recovered from the entry's offset).
+__device__ __forceinline__ const uint32_t* hist_base(const StepArgs& a, uint32_t hrow) {
+  return a.hist + (size_t)(a.hist_rows - 1u - hrow) * a.n_words;  // row of step t
 }
 
 template <bool BF16>
@@ -341,8 +339,9 @@ __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, ui
 // during the launch).  Returns the lane's hits.
 template <bool BF16>
 __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit un,
-                                              uint32_t hrow, uint32_t slot1) {
+                                              const uint32_t* hb, uint32_t slot1) {
   constexpr uint32_t B = 8;
+  const uint32_t pad = a.hist_rows * a.n_pad;
   const ProjDev& P = a.projs[un.proj];
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t hits = 0;
@@ -354,8 +353,7 @@ __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit 
     uint32_t hit = 0;
 #pragma unroll
     for (uint32_t u = 0; u < B; ++u)
-      if ((e[u] >> a.ell_shift) < a.hist_rows)
-        hit |= ((__ldcg(hist_word(a, hrow, e[u])) >> (e[u] & 31u)) & 1u) << u;
+      if (e[u] < pad) hit |= ((__ldcg(hb + (e[u] >> 5)) >> (e[u] & 31u)) & 1u) << u;
     hits += __popc(hit);
     while (hit) {
       const uint32_t u = __ffs(hit) - 1;
@@ -387,7 +385,8 @@ __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw,
   if (PULL && a.n_pull_units) {
     const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     uint32_t hits = 0;
-    for (uint32_t u = gw; u < a.n_pull_units; u += nw) hits += pull_unit<BF16>(a, a.pull_units[u], ix.hrow, slot1);
+    const uint32_t* hb = hist_base(a, ix.hrow);
+    for (uint32_t u = gw; u < a.n_pull_units; u += nw) hits += pull_unit<BF16>(a, a.pull_units[u], hb, slot1);
     hits = __reduce_add_sync(kFull, hits);
     if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
   }
@@ -453,9 +452,9 @@ __global__ void __launch_bounds__(kBlock) k_deliver(StepArgs a) {
 
 // Dense pull of the per-step driver (one 1,024-thread block per SM).  Each
 // block stages the summary rows of steps t + 1 - d, d = 1..H (one bit per
-// 32-cell word: did any cell of it spike) in shared memory, delay-major with
-// a power-of-two stride so an entry's summary word is s_sum[e >> 10]; row H
-// stays zero, so padding entries (delay field H) never pass.  Warps stream
+// 32-cell word: did any cell of it spike) in shared memory, delay-major, so
+// an entry's summary word is s_sum[e >> 10]; the word after them stays zero,
+// so padding entries (delay field H) never pass.  Warps stream
 // units (gw, gw + nw, ...; the first one's loads overlap the staging): a lane
 // loads its 32 entries of a unit at once, settles every entry whose summary
 // bit is clear in shared memory, and walks the few that passed four at a
@@ -466,7 +465,7 @@ template <bool BF16, bool SUM>
 __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
   constexpr uint32_t E = kPullUnit / 32;  // entries per lane per unit
   constexpr uint32_t W = 4;               // entries walked per trip
-  extern __shared__ uint32_t s_sum[];     // [H + 1][2^(ell_shift - 10)]
+  extern __shared__ uint32_t s_sum[];     // [H][n_swords] + 1 (padding's word)
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
@@ -481,18 +480,17 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
     for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
   }
   if (SUM) {
-    const uint32_t R = a.hist_rows + 1u, stride_log = a.ell_shift - 10u;
+    const uint32_t R = a.hist_rows + 1u;
     for (uint32_t d1 = 0; d1 < a.hist_rows; ++d1) {
       const uint32_t src = (ix.srow + R - d1) % R;  // row of step t - d1
       for (uint32_t j = threadIdx.x; j < a.n_swords; j += kPullBlock)
-        s_sum[(d1 << stride_log) + j] = __ldg(a.hsum + (size_t)src * a.n_swords + j);
+        s_sum[d1 * a.n_swords + j] = __ldg(a.hsum + (size_t)src * a.n_swords + j);
     }
-    if (threadIdx.x == 0) s_sum[a.hist_rows << stride_log] = 0u;  // padding's word
+    if (threadIdx.x == 0) s_sum[a.hist_rows * a.n_swords] = 0u;  // padding's word
     __syncthreads();
   }
-  // History word of entry e: row hrow + H - (delay - 1) of the doubled history.
-  const uint32_t* hist_top = a.hist + (size_t)(ix.hrow + a.hist_rows) * a.n_words;
-  const uint32_t gmask = (1u << a.ell_shift) - 1u;
+  const uint32_t* hb = hist_base(a, ix.hrow);
+  const uint32_t pad = a.hist_rows * a.n_pad;
   uint32_t hits = 0;
   for (uint32_t u = gw; u < n; u += nw) {
     const PullUnit un = a.pull_units[u];
@@ -509,7 +507,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
         const uint32_t sw = s_sum[e[k] >> 10];
         need |= (__funnelshift_r(sw, sw, e[k] >> 5) & 1u) << k;
       } else {
-        need |= (uint32_t)((e[k] >> a.ell_shift) < a.hist_rows) << k;
+        need |= (uint32_t)(e[k] < pad) << k;
       }
     }
     while (need) {
@@ -523,9 +521,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
       for (uint32_t j = 0; j < W; ++j) ev[j] = ks[j] < E ? __ldg(src + ks[j] * 32u) : 0u;
 #pragma unroll
       for (uint32_t j = 0; j < W; ++j)
-        hw[j] = ks[j] < E ? __ldg(hist_top - (size_t)(ev[j] >> a.ell_shift) * a.n_words +
-                                  ((ev[j] & gmask) >> 5))
-                          : 0u;
+        hw[j] = ks[j] < E ? __ldg(hb + (ev[j] >> 5)) : 0u;
 #pragma unroll
       for (uint32_t j = 0; j < W; ++j) {
         if (ks[j] < E && ((hw[j] >> (ev[j] & 31u)) & 1u)) {
@@ -641,12 +637,15 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
   const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kPersistBlock) >> 5;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
-  const bool has = gw < a.n_upd_words;
+  // Words are dealt round-robin over the blocks (word slot = warp x blocks +
+  // block), so every SM holds about the same number of cells and spikes.
+  const uint32_t ws = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  const bool has = ws < a.n_upd_words;
   uint32_t w = 0, seg = 0, i = 0, local = 0, mask = 0, r0 = 0, r1 = 0, od = 0;
   bool valid = false, lif = false;
   float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
   if (has) {
-    w = __ldg(a.upd_words + gw);
+    w = __ldg(a.upd_words + ws);
     seg = __ldg(a.seg_of_word + w);
     i = (w << 5) + lane;
     const SegDev& sd = a.segs[seg];
@@ -710,14 +709,16 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   const unsigned long long t0 = ix.t;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t wib = threadIdx.x >> 5;
-  const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
-  const bool has = gw < a.n_upd_words;
+  // Words are dealt round-robin over the blocks (word slot = warp x blocks +
+  // block), so every SM holds about the same number of cells and spikes.
+  const uint32_t ws = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+  const bool has = ws < a.n_upd_words;
   uint32_t w = 0, seg = 0, i = 0, local = 0, mask = 0, r0 = 0, r1 = 0, od = 0;
   bool valid = false, lif = false;
   float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
   if (has) {
-    w = __ldg(a.upd_words + gw);
+    w = __ldg(a.upd_words + ws);
     seg = __ldg(a.seg_of_word + w);
     i = (w << 5) + lane;
     const SegDev& sd = a.segs[seg];
@@ -837,9 +838,7 @@ cudaError_t launch_deliver(const StepArgs& a, int blocks, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-size_t pull_sum_bytes(const StepArgs& a) {
-  return (size_t)(a.hist_rows + 1u) << (a.ell_shift - 10u + 2u);
-}
+size_t pull_sum_bytes(const StepArgs& a) { return ((size_t)a.hist_rows * a.n_swords + 1) * 4; }
 
 static size_t pull_smem_bytes(const StepArgs& a) { return a.pull_sum ? pull_sum_bytes(a) : 0; }
 
@@ -899,14 +898,6 @@ int persistent_kernel_kind(const StepArgs& a, int blocks) {
   return a.n_pull_units == 0 ? SGB_KERNEL_FUSED : SGB_KERNEL_RESIDENT;
 }
 
-// Register-resident kernels need one warp per word and no more: fewer blocks
-// mean fewer arrivals at every grid barrier.
-static int persistent_grid(const StepArgs& a, int blocks, int kind) {
-  if (kind == SGB_KERNEL_GENERAL) return blocks;
-  const int need = (int)((a.n_upd_words + kPersistBlock / 32 - 1) / (kPersistBlock / 32));
-  return need < 1 ? 1 : (need < blocks ? need : blocks);
-}
-
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s) {
   StepArgs args = a;
   uint32_t n = n_steps;
@@ -920,8 +911,7 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                                         : (const void*)k_persistent_resident<false>)
                               : (a.bf16 ? (const void*)k_persistent<true>
                                         : (const void*)k_persistent<false>);
-  return cudaLaunchCooperativeKernel(fn, dim3(persistent_grid(a, blocks, kind)), dim3(kPersistBlock),
-                                     params, 0, s);
+  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, 0, s);
 }
 
 }  // namespace sgb

@@ -106,15 +106,17 @@ constexpr uint32_t kIndexBits = 28;
 constexpr uint32_t kIndexMask = (1u << kIndexBits) - 1u;
 constexpr int kMaxDelay = 15;
 
-// Dense-pull (ELL) entry: the pre cell's global (padded) index g in the low
-// `shift` bits and delay - 1 above them, so the entry names the spike bit of
-// step t + 1 - d directly.  shift = 10 + log2 of the spike-summary row stride
-// (a power of two >= the summary words per row), which makes e >> 10 the
-// entry's summary word and (e >> 5) & 31 its bit there.  Padding carries the
-// delay field H (one past the deepest delay): ell_pad(H, shift).
-SGB_HD uint32_t ell_entry(uint32_t g, uint32_t delay, uint32_t shift) {
-  return ((delay - 1u) << shift) | g;
+// Dense-pull (ELL) entry: (delay - 1) * n_pad + g for the pre cell's global
+// (padded) index g, with n_pad a multiple of 1,024.  The spike history keeps
+// its rows in decreasing step order (and twice, so no wrap), so the history
+// word of the pre cell at step t + 1 - d sits at base_t + (e >> 5), its bit
+// is e & 31, and, with the summary rows of steps t, t - 1, ... laid out the
+// same way at one bit per history word, its summary word is e >> 10 and the
+// bit there (e >> 5) & 31.  Padding carries delay field H, one past the
+// deepest delay: ell_pad = H * n_pad.
+SGB_HD uint32_t ell_entry(uint32_t g, uint32_t delay, uint32_t n_pad) {
+  return (delay - 1u) * n_pad + g;
 }
-SGB_HD uint32_t ell_pad(uint32_t hist_rows, uint32_t shift) { return hist_rows << shift; }
+SGB_HD uint32_t ell_pad(uint32_t hist_rows, uint32_t n_pad) { return hist_rows * n_pad; }
 
 }  // namespace sgb
