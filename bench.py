@@ -337,7 +337,7 @@ def run_gb300(a):
             pg.destroy_process_group()
         return
     # Roofline of the kernel that ran the timed region.  Algorithmic bytes:
-    # per LIF cell and step 16 B state read + 16 B write + 8 B ring slot; per
+    # per LIF cell and step 12 B state read + 12 B write + 8 B ring slot; per
     # input cell 4 B source mask; 8 B per 32-cell bitmap word (two history
     # copies); per delivered push synapse 4 B word + W B weight + 8 B atomic
     # read-modify-write; per dense entry and step 4 B, plus W + 8 B per entry
@@ -348,7 +348,7 @@ def run_gb300(a):
     n_words = sum((sg_.count + 31) // 32 for sg_ in segs)
     wbytes = 2 if wl["bf16"] else 4
     info1 = sim.info()
-    upd_step = 40 * n_lif + 4 * n_in + 8 * n_words + 4 * info_t.pull_entries
+    upd_step = 32 * n_lif + 4 * n_in + 8 * n_words + 4 * info_t.pull_entries
     alg_bytes = (a.steps * a.chunk * upd_step + (dlv1 - dlv0) * (12 + wbytes) +
                  (info_t.pulled - pull0) * (8 + wbytes))
     peak, peak_kind = measured_hbm()

@@ -120,7 +120,8 @@ struct StepArgs {
   const uint32_t* push_syn;
   const void* push_w;
   const PullUnit* pull_units;
-  float4* state;
+  float* su;                      // potential, or the refractory count (pack_u)
+  float2* sg;                     // conductances of channels 0 and 1
   int* ring;                      // int2 per cell per slot, viewed as int[2]
   uint32_t* hist;                 // [2H][n_words]: rows H-1-(t mod H) and 2H-1-(t mod H) hold step t
   uint32_t* hsum;                 // [H + 1][n_swords]: bit w of row t mod (H + 1) = word w

@@ -57,7 +57,7 @@ static void fill_lif(SegDev& d, const Population& p, double dt, int substeps) {
   d.dt_cm = (float)(dt / (double)p.Cm);
   // Reference: ref_step = (int)(target.dt_ref / DT) with DT a double literal
   // (Simulation_header.cu:322).
-  d.ref_steps = (int32_t)((double)p.dt_ref / dt);
+  d.ref_steps = (int32_t)((double)p.dt_ref / dt);  // at most kRefMax (checked at create)
   d.substeps = substeps;
   for (int c = 0; c < 2; ++c) {
     if (c < p.c_num) {
@@ -281,7 +281,12 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       d.key_base = key;
       d.kind = p.dev_type == SGB_INPUT ? kSegInput : kSegLif;
       d.seed = s.seeds[ni];
-      if (d.kind == kSegLif) fill_lif(d, p, cfg.dt_ms, cfg.substeps);
+      if (d.kind == kSegLif) {
+        fill_lif(d, p, cfg.dt_ms, cfg.substeps);
+        if (d.ref_steps > kRefMax)
+          return set_error(SGB_ERR_RANGE, "population %zu: refractory period of %d steps exceeds %d",
+                           pi, d.ref_steps, kRefMax);
+      }
       d.inv_scale[0] = ldexpf(1.0f, -bits[pi * 2 + 0]);
       d.inv_scale[1] = ldexpf(1.0f, -bits[pi * 2 + 1]);
       s.segs.push_back(d);
@@ -439,7 +444,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   const size_t o_outdeg = take((size_t)s.n_pad * 4);
   const size_t o_words = take(std::max<size_t>(upd_words.size(), 1) * 4);
   const size_t o_units = take(std::max<size_t>(cap_units, 1) * sizeof(PullUnit));
-  const size_t o_state = take((size_t)s.n_pad * sizeof(float4));
+  const size_t o_su = take((size_t)s.n_pad * sizeof(float));
+  const size_t o_sg = take((size_t)s.n_pad * sizeof(float2));
   const size_t o_ring = take((size_t)s.ring_slots * s.n_pad * 8);
   // Spike history (two copies of H rows) followed by its summary (H + 1 rows
   // of one bit per word): one region, cleared and snapshotted together.
@@ -469,7 +475,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.outdeg = (const uint32_t*)(mb + o_outdeg);
   a.upd_words = (const uint32_t*)(mb + o_words);
   a.pull_units = (const PullUnit*)(mb + o_units);
-  a.state = (float4*)(mb + o_state);
+  a.su = (float*)(mb + o_su);
+  a.sg = (float2*)(mb + o_sg);
   a.ring = (int*)(mb + o_ring);
   a.hist = (uint32_t*)(mb + o_hist);
   a.hsum = a.hist + (size_t)2 * s.hist_rows * s.n_words;
@@ -531,15 +538,16 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
     SGB_CUDA(cudaMemcpyAsync((void*)s.args.segs, s.segs.data(), s.segs.size() * sizeof(SegDev),
                              cudaMemcpyHostToDevice, s.stream));
   }
-  std::vector<float4> st(s.n_pad, make_float4(0.f, 0.f, 0.f, 0.f));
+  std::vector<float> su(s.n_pad, 0.f);
   for (size_t si = 0; si < s.segs.size(); ++si) {
     const SegDev& d = s.segs[si];
     if (d.kind != kSegLif) continue;
     const Population& p = s.nets[s.seg_net[si]].pops[s.seg_pop[si]];
-    for (uint32_t j = 0; j < d.count; ++j) st[d.base + j].x = initial_u(p, d.seed, d.key_base + j);
+    for (uint32_t j = 0; j < d.count; ++j) su[d.base + j] = initial_u(p, d.seed, d.key_base + j);
   }
   const StepArgs& a = s.args;
-  SGB_CUDA(cudaMemcpyAsync(a.state, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaMemcpyAsync(a.su, su.data(), su.size() * sizeof(float), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaMemsetAsync(a.sg, 0, (size_t)s.n_pad * sizeof(float2), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ring, 0, (size_t)s.ring_slots * s.n_pad * 8, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.hist, 0, s.hist_bytes, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
@@ -726,43 +734,58 @@ int sim_set_rates(Sim& s, int32_t net, int32_t n, const float* rates) {
 }
 
 int sim_get_state(Sim& s, float* u, float* g, int32_t* ref) {
-  std::vector<float4> st(s.n_pad);
-  SGB_CUDA(cudaMemcpyAsync(st.data(), s.args.state, st.size() * sizeof(float4), cudaMemcpyDeviceToHost, s.stream));
+  std::vector<float> su(s.n_pad);
+  std::vector<float2> sg(s.n_pad);
+  SGB_CUDA(cudaMemcpyAsync(su.data(), s.args.su, su.size() * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
+  SGB_CUDA(cudaMemcpyAsync(sg.data(), s.args.sg, sg.size() * sizeof(float2), cudaMemcpyDeviceToHost, s.stream));
   SGB_CUDA(cudaStreamSynchronize(s.stream));
   for (size_t si = 0; si < s.segs.size(); ++si) {
     const SegDev& d = s.segs[si];
     const int64_t f = s.seg_first_id[si];
+    const bool lif = d.kind == kSegLif;
     for (uint32_t j = 0; j < d.count; ++j) {
-      const float4 v = st[d.base + j];
-      int32_t r;
-      memcpy(&r, &v.w, 4);
-      if (u) u[f + j] = v.x;
-      if (g) { g[2 * (f + j)] = v.y; g[2 * (f + j) + 1] = v.z; }
+      const float x = su[d.base + j];
+      const int32_t r = lif ? unpack_ref(x) : 0;
+      if (u) u[f + j] = r ? d.Vr : x;
+      if (g) { g[2 * (f + j)] = sg[d.base + j].x; g[2 * (f + j) + 1] = sg[d.base + j].y; }
       if (ref) ref[f + j] = r;
     }
   }
   return SGB_OK;
 }
 
+// A refractory cell's potential is V_reset (the update pins it there and the
+// stored state keeps only the count), so a state with ref > 0 and another
+// potential is refused.
 int sim_set_state(Sim& s, const float* u, const float* g, const int32_t* ref) {
-  std::vector<float4> st(s.n_pad);
-  SGB_CUDA(cudaMemcpyAsync(st.data(), s.args.state, st.size() * sizeof(float4), cudaMemcpyDeviceToHost, s.stream));
+  std::vector<float> su(s.n_pad);
+  std::vector<float2> sg(s.n_pad);
+  SGB_CUDA(cudaMemcpyAsync(su.data(), s.args.su, su.size() * sizeof(float), cudaMemcpyDeviceToHost, s.stream));
+  SGB_CUDA(cudaMemcpyAsync(sg.data(), s.args.sg, sg.size() * sizeof(float2), cudaMemcpyDeviceToHost, s.stream));
   SGB_CUDA(cudaStreamSynchronize(s.stream));
   for (size_t si = 0; si < s.segs.size(); ++si) {
     const SegDev& d = s.segs[si];
     if (d.kind != kSegLif) continue;
     const int64_t f = s.seg_first_id[si];
     for (uint32_t j = 0; j < d.count; ++j) {
-      float4& v = st[d.base + j];
-      if (u) v.x = u[f + j];
-      if (g) { v.y = g[2 * (f + j)]; v.z = g[2 * (f + j) + 1]; }
+      float& x = su[d.base + j];
+      int32_t r = unpack_ref(x);
+      float v = r ? d.Vr : x;
+      if (u) v = u[f + j];
       if (ref) {
-        if (ref[f + j] < 0) return set_error(SGB_ERR_ARG, "negative refractory count");
-        memcpy(&v.w, &ref[f + j], 4);
+        if (ref[f + j] < 0 || ref[f + j] > kRefMax)
+          return set_error(SGB_ERR_ARG, "refractory count %d out of 0..%d", ref[f + j], kRefMax);
+        r = ref[f + j];
       }
+      if (r > 0 && v != d.Vr)
+        return set_error(SGB_ERR_ARG, "cell %lld is refractory but its potential is not V_reset",
+                         (long long)(f + j));
+      x = pack_u(v, r);
+      if (g) sg[d.base + j] = make_float2(g[2 * (f + j)], g[2 * (f + j) + 1]);
     }
   }
-  SGB_CUDA(cudaMemcpyAsync(s.args.state, st.data(), st.size() * sizeof(float4), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaMemcpyAsync(s.args.su, su.data(), su.size() * sizeof(float), cudaMemcpyHostToDevice, s.stream));
+  SGB_CUDA(cudaMemcpyAsync(s.args.sg, sg.data(), sg.size() * sizeof(float2), cudaMemcpyHostToDevice, s.stream));
   SGB_CUDA(cudaStreamSynchronize(s.stream));
   return SGB_OK;
 }
@@ -881,15 +904,15 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   }
   // Snapshot of the device state a run changes.
   const StepArgs& a = s.args;
-  const size_t b_state = (size_t)s.n_pad * sizeof(float4);
+  const size_t b_su = (size_t)s.n_pad * sizeof(float), b_sg = (size_t)s.n_pad * sizeof(float2);
   const size_t b_ring = (size_t)s.ring_slots * s.n_pad * 8;
   const size_t b_hist = s.hist_bytes;
   const size_t b_tot = s.segs.size() * sizeof(double);
-  const size_t total = b_state + b_ring + b_hist + sizeof(Ctl) + b_tot;
+  const size_t total = b_su + b_sg + b_ring + b_hist + sizeof(Ctl) + b_tot;
   char* snap = nullptr;
   SGB_CUDA(cudaMalloc(&snap, total));
   auto save = [&](bool restore) -> cudaError_t {
-    struct { void* dev; size_t n; } parts[5] = {{a.state, b_state}, {a.ring, b_ring}, {a.hist, b_hist},
+    struct { void* dev; size_t n; } parts[6] = {{a.su, b_su}, {a.sg, b_sg}, {a.ring, b_ring}, {a.hist, b_hist},
                                               {a.ctl, sizeof(Ctl)}, {a.totals, b_tot}};
     size_t o = 0;
     for (auto& p : parts) {
@@ -969,14 +992,14 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
   constexpr int K = SGB_KCLASS_COUNT;
   const StepArgs& a = s.args;
   const double W = s.bf16 ? 2.0 : 4.0;
-  // Algorithmic bytes: update = state 16 B read + 16 B write + ring 8 B per
+  // Algorithmic bytes: update = state 12 B read + 12 B write + ring 8 B per
   // LIF cell, mask 4 B per input cell, 8 B per bitmap word (two history
   // copies), 8 B per push item written; deliver = per walked push synapse 4 B
   // word + W weight + 8 B atomic, 8 B per push item read; pull = 4 B per
   // stored dense entry plus, per entry whose pre cell spiked, W weight + 8 B
   // atomic.
   double upd_bytes = (double)a.n_words * 8.0;
-  for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 40.0 * d.count : 4.0 * d.count;
+  for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 32.0 * d.count : 4.0 * d.count;
   double pull_entries = 0;
   for (const ProjDev& P : s.projs)
     if (P.mode == SGB_PROP_ELL) pull_entries += (double)P.ell_n;

@@ -220,7 +220,8 @@ __device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint
 // cells.  Callers may issue load_word for the next word before finishing the
 // current one (the two touch different cells).
 struct WordIn {
-  float4 st;
+  float u;
+  float2 g;
   int2 acc;
   uint32_t seg;
 };
@@ -230,8 +231,19 @@ __device__ __forceinline__ WordIn load_word(const StepArgs& a, uint32_t w, const
   WordIn in;
   in.seg = __ldg(a.seg_of_word + w);
   in.acc = __ldcg(reinterpret_cast<const int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i);
-  in.st = a.state[i];
+  in.u = a.su[i];
+  in.g = a.sg[i];
   return in;
+}
+
+// Register state {u, g0, g1, ref bits} from / to the stored fields.
+__device__ __forceinline__ float4 state_in(float u, float2 g, float vr) {
+  const int32_t ref = unpack_ref(u);
+  return make_float4(ref ? vr : u, g.x, g.y, __int_as_float(ref));
+}
+__device__ __forceinline__ void state_out(const StepArgs& a, uint32_t i, const float4& st) {
+  a.su[i] = pack_u(st.x, __float_as_int(st.w));
+  a.sg[i] = make_float2(st.y, st.z);
 }
 
 __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
@@ -250,9 +262,9 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
     } else {
       if (in.acc.x | in.acc.y)
         __stcg(reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i, make_int2(0, 0));
-      float4 st = in.st;
+      float4 st = state_in(in.u, in.g, sd.Vr);
       fired = lif_update(sd, a.substeps, st, in.acc);
-      a.state[i] = st;
+      state_out(a, i, st);
     }
   }
   uint32_t r0 = 0, r1 = 0, od = 0;
@@ -653,7 +665,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     valid = local < sd.count;
     lif = sd.kind == kSegLif;
     if (valid) {
-      if (lif) st = a.state[i]; else mask = __ldg(a.src_mask + i);
+      if (lif) st = state_in(a.su[i], a.sg[i], sd.Vr); else mask = __ldg(a.src_mask + i);
       od = __ldg(a.outdeg + i);
       if (a.any_push) {
         r0 = __ldg(a.push_row + i);
@@ -680,7 +692,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
     ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
-  if (valid && lif) a.state[i] = st;
+  if (valid && lif) state_out(a, i, st);
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
@@ -726,7 +738,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     valid = local < sd.count;
     lif = sd.kind == kSegLif;
     if (valid) {
-      if (lif) st = a.state[i]; else mask = __ldg(a.src_mask + i);
+      if (lif) st = state_in(a.su[i], a.sg[i], sd.Vr); else mask = __ldg(a.src_mask + i);
       od = __ldg(a.outdeg + i);
       r0 = __ldg(a.push_row + i);
       r1 = __ldg(a.push_row + i + 1);
@@ -805,7 +817,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
     ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
-  if (valid && lif) a.state[i] = st;
+  if (valid && lif) state_out(a, i, st);
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {

@@ -106,6 +106,26 @@ constexpr uint32_t kIndexBits = 28;
 constexpr uint32_t kIndexMask = (1u << kIndexBits) - 1u;
 constexpr int kMaxDelay = 15;
 
+// Stored LIF state: the potential u (4 B) and the two conductances (8 B).
+// A cell that is refractory after a step sits at V_reset (the update pins it
+// there), so its potential field carries the refractory count instead, as a
+// quiet-NaN payload: 0x7FC00000 | ref, ref in 1..2^22 - 1.  Arithmetic NaNs
+// have an empty payload and read back as themselves with ref 0.
+constexpr uint32_t kRefTag = 0x7FC00000u;
+constexpr int32_t kRefMax = (1 << 22) - 1;
+SGB_HD float pack_u(float u, int32_t ref) {
+  union { float f; uint32_t b; } v;
+  if (ref > 0) { v.b = kRefTag | (uint32_t)ref; return v.f; }
+  return u;
+}
+// Unpacks the potential field: the refractory count (0 if none) and the
+// potential (vr while refractory).
+SGB_HD int32_t unpack_ref(float x) {
+  union { float f; uint32_t b; } v;
+  v.f = x;
+  return v.b - (kRefTag + 1u) < (uint32_t)kRefMax ? (int32_t)(v.b - kRefTag) : 0;
+}
+
 // Dense-pull (ELL) entry: (delay - 1) * n_pad + g for the pre cell's global
 // (padded) index g, with n_pad a multiple of 1,024.  The spike history keeps
 // its rows in decreasing step order (and twice, so no wrap), so the history
