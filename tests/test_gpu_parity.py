@@ -66,6 +66,27 @@ def test_c1_full_bit_exact_mixed_modes(exec_mode):
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
 
 
+@pytest.mark.parametrize("prop", [sg.PROP_CSR, sg.PROP_ELL])
+@pytest.mark.parametrize("exec_mode", [sg.EXEC_GRAPH, sg.EXEC_PERSISTENT])
+def test_large_net_general_kernels(prop, exec_mode):
+    """Config 1 at 20x population size (185k cells, more 32-cell words than a
+    grid of resident warps): the general persistent kernel (two barriers a
+    step) or, per step, k_update + k_pull + k_deliver with the staged spike
+    summary; bit-exact either way."""
+    net = sg.scaffold(1, 20.0, 21)
+    steps = 240
+    sim = sg.Simulation([net], [21], default_prop=prop, exec_mode=exec_mode, raster=True,
+                        chunk_steps=120)
+    if exec_mode == sg.EXEC_PERSISTENT:
+        assert sim.info().step_kernel == 1  # SGB_KERNEL_GENERAL
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
+    exp = _oracle(net, 21, steps)
+    _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    if prop == sg.PROP_ELL:
+        assert sim.info().pulled > 0
+    sim.close()
+
+
 def test_batched_instances_match_standalone():
     """Three instances of different size and seed in one handle: each equals its own oracle."""
     seeds = [5, 6, 9]
