@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--exec", default="persistent", choices=["persistent", "graph"])
     ap.add_argument("--no-ell-roofline", action="store_true")
     ap.add_argument("--blocks-per-sm", type=int, default=1)
+    ap.add_argument("--no-l2-persist", action="store_true",
+                    help="plain L2 caching of the cell state (no persisting window)")
     ap.add_argument("--autotune", action="store_true",
                     help="run the propagation/driver autotuner before timing (default for c5)")
     return ap.parse_args()
@@ -264,7 +266,7 @@ def run_gb300(a):
     exec_mode = sg.EXEC_PERSISTENT if a.exec == "persistent" else sg.EXEC_GRAPH
     sim = sg.Simulation(nets, seeds, weight_type=sg.WEIGHT_BF16 if wl["bf16"] else sg.WEIGHT_FP32,
                         chunk_steps=a.chunk, device=local, exec_mode=exec_mode,
-                        blocks_per_sm=a.blocks_per_sm)
+                        blocks_per_sm=a.blocks_per_sm, l2_persist=not a.no_l2_persist)
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
     tuned = None
@@ -396,7 +398,9 @@ def run_gb300(a):
                                    f"autotuned: {tuned['ell']} projections dense ELL pull, "
                                    f"{tuned['csr']} event-driven CSR push (instance 0)"),
                    "exec_kernel": sg._lib.KERNEL_NAMES.get(info.step_kernel, "?"),
-                   "l2": "flushed (256 MiB write) between timed steps",
+                   "l2": "flushed (256 MiB write) between timed steps; the cell-state window "
+                         "kept in persisting L2 is not evicted by the flush (resident by design)",
+                   "l2_persist_bytes": info.l2_persist_bytes,
                    "parallelism": f"replicas x{world}"},
         "synaptic_events_per_s": events_all / (ms_max / 1000.0),
         "gpu_launches": launches,

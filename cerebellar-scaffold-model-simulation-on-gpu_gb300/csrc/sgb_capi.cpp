@@ -34,6 +34,7 @@ void sgb_config_init(sgb_config* cfg) {
   cfg->default_prop = SGB_PROP_AUTO;
   cfg->raster = 0;
   cfg->blocks_per_sm = 0;
+  cfg->l2_persist = 1;
 }
 
 const char* sgb_last_error(void) { return last_error(); }
@@ -292,6 +293,7 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
   info->events = (int64_t)ctl.events;
   info->delivered = (int64_t)ctl.delivered;
   info->pulled = (int64_t)ctl.pulled;
+  info->l2_persist_bytes = (int64_t)s.l2_setaside;
   for (const ProjDev& P : s.projs)
     if (P.mode == SGB_PROP_ELL) info->pull_entries += P.ell_n;
   info->step_kernel = s.cfg.exec_mode == SGB_EXEC_PERSISTENT

@@ -33,8 +33,27 @@ namespace sgb {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Access-policy window of the cell state on stream st (num_bytes 0 clears it).
+static cudaError_t l2_window_on(const Sim& s, cudaStream_t st, bool on) {
+  cudaStreamAttrValue v;
+  memset(&v, 0, sizeof v);
+  v.accessPolicyWindow.base_ptr = s.l2_base;
+  v.accessPolicyWindow.num_bytes = on ? s.l2_window : 0;
+  v.accessPolicyWindow.hitRatio = on ? s.l2_hit : 0.f;
+  v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+  v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  return cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &v);
+}
+
 Sim::~Sim() {
   if (stream) cudaStreamSynchronize(stream);
+  if (l2_window) {
+    // Hand the set-aside back: clear the window, demote persisting lines and
+    // restore the context's previous limit.
+    l2_window_on(*this, stream, false);
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, l2_prev_limit);
+  }
   for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
   if (d_ell) cudaFree(d_ell);
   if (d_push) cudaFree(d_push);
@@ -500,6 +519,26 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.bf16 = s.bf16 ? 1 : 0;
   a.substeps = cfg.substeps;
   s.deliver_blocks = 2 * s.sm_count;
+  // The cell state is read and rewritten every step; where the device lets
+  // this context set L2 aside for persisting accesses, the state window
+  // stays in L2 across steps while ring slots, tables and history stream
+  // past it.  The limit is a property of this process's context.
+  if (cfg.l2_persist) {
+    int maxp = 0, maxw = 0;
+    cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, cfg.device);
+    cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, cfg.device);
+    const size_t region = (size_t)((char*)(a.sg + s.n_pad) - (char*)a.su);
+    if (maxp > 0 && maxw > 0 && region > 0) {
+      SGB_CUDA(cudaDeviceGetLimit(&s.l2_prev_limit, cudaLimitPersistingL2CacheSize));
+      const size_t want = std::min(region, (size_t)maxp);
+      if (want > s.l2_prev_limit) SGB_CUDA(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want));
+      SGB_CUDA(cudaDeviceGetLimit(&s.l2_setaside, cudaLimitPersistingL2CacheSize));
+      s.l2_base = a.su;
+      s.l2_window = std::min(region, (size_t)maxw);
+      s.l2_hit = (float)std::min(1.0, (double)s.l2_setaside / (double)s.l2_window);
+      SGB_CUDA(l2_window_on(s, s.stream, true));
+    }
+  }
   SGB_CUDA(pull_setup());
   s.pull_blocks = pull_blocks_per_sm(a) * s.sm_count;
   const int bpsm = std::min(cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : 1,
@@ -808,7 +847,14 @@ int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
 
 int sim_set_stream(Sim& s, cudaStream_t st) {
   SGB_CUDA(cudaStreamSynchronize(s.stream));
-  s.stream = st ? st : s.own_stream;
+  cudaStream_t next = st ? st : s.own_stream;
+  if (s.l2_window && next != s.stream) {
+    // The state window follows the handle's launches; a caller's stream is
+    // left without it once the handle moves on.
+    if (s.stream != s.own_stream) SGB_CUDA(l2_window_on(s, s.stream, false));
+    SGB_CUDA(l2_window_on(s, next, true));
+  }
+  s.stream = next;
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
   return SGB_OK;

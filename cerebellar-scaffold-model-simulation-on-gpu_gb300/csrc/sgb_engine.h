@@ -55,6 +55,10 @@ struct Sim {
   int pull_blocks = 0;        // k_pull grid (resident blocks per SM x SMs)
   size_t hist_bytes = 0;      // spike history + its summary
   int persistent_blocks = 0;
+  // Persisting L2 window over the cell state (su, sg).
+  void* l2_base = nullptr;
+  size_t l2_window = 0, l2_setaside = 0, l2_prev_limit = 0;
+  float l2_hit = 0.f;
   SrcDev* h_srcs = nullptr;  // pinned staging of the source table
 
   // Host staging for outputs.

@@ -37,7 +37,7 @@ class Config(C.Structure):
     _fields_ = [("dt_ms", C.c_double), ("substeps", C.c_int32), ("weight_type", C.c_int32),
                 ("exec_mode", C.c_int32), ("chunk_steps", C.c_int32), ("device", C.c_int32),
                 ("default_prop", C.c_int32), ("raster", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("reserved", C.c_int32 * 8)]
+                ("l2_persist", C.c_int32), ("reserved", C.c_int32 * 7)]
 
 
 class InputParams(C.Structure):
@@ -77,7 +77,7 @@ class SimInfo(C.Structure):
                 ("weight_type", C.c_int32), ("substeps", C.c_int32), ("chunk_steps", C.c_int32),
                 ("dt_ms", C.c_double), ("events", C.c_int64), ("delivered", C.c_int64),
                 ("step_kernel", C.c_int32), ("reserved_", C.c_int32), ("pulled", C.c_int64),
-                ("pull_entries", C.c_int64)]
+                ("pull_entries", C.c_int64), ("l2_persist_bytes", C.c_int64)]
 
 
 P = C.POINTER

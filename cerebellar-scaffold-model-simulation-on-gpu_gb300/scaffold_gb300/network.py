@@ -220,7 +220,8 @@ class Simulation:
     def __init__(self, nets: Sequence[Network], seeds: Sequence[int] | None = None, *,
                  dt_ms: float = 0.1, substeps: int = 1, weight_type: int = L.WEIGHT_FP32,
                  exec_mode: int = L.EXEC_GRAPH, chunk_steps: int = 1000, device: int = 0,
-                 default_prop: int = L.PROP_AUTO, raster: bool = False, blocks_per_sm: int = 0):
+                 default_prop: int = L.PROP_AUTO, raster: bool = False, blocks_per_sm: int = 0,
+                 l2_persist: bool = True):
         cfg = L.Config()
         L.lib().sgb_config_init(C.byref(cfg))
         cfg.dt_ms = dt_ms
@@ -232,6 +233,7 @@ class Simulation:
         cfg.default_prop = default_prop
         cfg.raster = 1 if raster else 0
         cfg.blocks_per_sm = blocks_per_sm
+        cfg.l2_persist = 1 if l2_persist else 0
         self.nets = list(nets)
         n = len(self.nets)
         arr = (C.c_void_p * n)(*[x.handle.value for x in self.nets])

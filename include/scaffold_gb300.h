@@ -88,7 +88,9 @@ typedef struct sgb_config {
   int32_t default_prop;  /* mode for projections added with SGB_PROP_AUTO                */
   int32_t raster;        /* 1: record every spike for sgb_sim_run's raster output        */
   int32_t blocks_per_sm; /* persistent driver: resident blocks per SM (0: 1)              */
-  int32_t reserved[8];
+  int32_t l2_persist;    /* 1 (default): keep the cell state in a persisting L2 window    */
+                         /* (within this process's context); 0: plain caching          */
+  int32_t reserved[7];
 } sgb_config;
 
 typedef struct sgb_input_params {
@@ -137,6 +139,7 @@ typedef struct sgb_sim_info {
   int32_t reserved_;
   int64_t pulled;        /* dense-pull entries whose pre cell had spiked (deliveries) since the last reset */
   int64_t pull_entries;  /* dense-table entries streamed per step (0 without dense projections) */
+  int64_t l2_persist_bytes; /* L2 set aside for the persisting state window (0: none)   */
 } sgb_sim_info;
 
 /* Step kernels (sgb_sim_info.step_kernel). */
