@@ -203,7 +203,14 @@ def ell_roofline(peak: float):
     info = sim.info()
     sim.close()
     gbs = bytes_pl[2] / (mean_us[2] * 1e-6) / 1e9
-    return {"kernel": "k_pull (dense ELL pull, every projection)", "workload":
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dense_ell", {}).get("k_pull")
+        except ValueError:
+            traffic = None
+    return {"kernel": "k_pull (dense ELL pull, every projection)", "traffic": traffic, "workload":
             f"config 5: 4 seeds, {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
             "mean_us": mean_us[2], "bytes_per_launch": bytes_pl[2], "achieved": gbs,
             "unit": "GB/s", "peak": peak, "frac": gbs / peak,
