@@ -183,6 +183,26 @@ def cpu_baseline(wl: dict, sample_steps: int):
                       f"OpenMP over post cells"}
 
 
+def stream_read_gbs(nbytes: int, reps: int = 20) -> float:
+    """Read bandwidth of a plain device reduction (torch sum) over a buffer of
+    the same size: what streaming alone reaches for a launch of this size."""
+    import torch
+
+    x = torch.ones(nbytes // 4, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        x.sum()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        x.sum()
+    e1.record()
+    torch.cuda.synchronize()
+    gbs = nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del x
+    return gbs
+
+
 def ell_roofline(peak: float):
     """Dense ELL pull at HBM scale: config 5 (4 batched seeds of the ~925k-cell
     scaffold, 109M synapses, 437 MB of ELL entries, larger than L2) with every
@@ -203,6 +223,7 @@ def ell_roofline(peak: float):
     info = sim.info()
     sim.close()
     gbs = bytes_pl[2] / (mean_us[2] * 1e-6) / 1e9
+    ceiling = stream_read_gbs(int(info.pull_entries) * 4)
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
@@ -214,6 +235,7 @@ def ell_roofline(peak: float):
             f"config 5: 4 seeds, {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
             "mean_us": mean_us[2], "bytes_per_launch": bytes_pl[2], "achieved": gbs,
             "unit": "GB/s", "peak": peak, "frac": gbs / peak,
+            "stream_read_gbs_same_bytes": ceiling,
             "l2": "entries 437 MB per launch (not L2-resident); no flush between launches"}
 
 
