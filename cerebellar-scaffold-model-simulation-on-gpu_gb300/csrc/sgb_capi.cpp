@@ -213,6 +213,24 @@ int sgb_net_input_ids(const sgb_net* net, int32_t src, uint32_t* ids) {
   return SGB_OK;
 }
 
+int sgb_net_add_plasticity(sgb_net* net, int32_t proj, const sgb_plasticity_params* params) {
+  if (!net) return set_error(SGB_ERR_ARG, "net is NULL");
+  SGB_GUARD(return add_plasticity(net->net, proj, params);)
+}
+
+int sgb_net_plasticity_info(const sgb_net* net, int32_t proj, int32_t* plastic,
+                            sgb_plasticity_params* params) {
+  if (!net || !plastic) return set_error(SGB_ERR_ARG, "NULL argument");
+  if (proj < 0 || proj >= (int32_t)net->net.projs.size())
+    return set_error(SGB_ERR_ARG, "projection %d out of range", proj);
+  const Projection& pr = net->net.projs[proj];
+  *plastic = pr.plastic ? 1 : 0;
+  if (params) {
+    if (pr.plastic) *params = pr.plast; else memset(params, 0, sizeof *params);
+  }
+  return SGB_OK;
+}
+
 int sgb_net_write_projection_dat(const sgb_net* net, int32_t proj, const char* path) {
   if (!net || !path) return set_error(SGB_ERR_ARG, "net or path is NULL");
   SGB_GUARD(return write_projection_dat(net->net, proj, path);)
@@ -351,6 +369,11 @@ int sgb_sim_get_propagation(const sgb_sim* sim, int32_t net, int32_t proj, int32
     return set_error(SGB_ERR_ARG, "projection %d out of range", proj);
   *mode = (int32_t)s.projs[s.net_proj0[net] + proj].mode;
   return SGB_OK;
+}
+
+int sgb_sim_plastic_values(sgb_sim* sim, int32_t net, int32_t proj, float* values) {
+  SIM_CHECK(sim);
+  SGB_GUARD(return sim_plastic_values(*sim->sim, net, proj, values);)
 }
 
 int sgb_sim_autotune(sgb_sim* sim, int32_t n_steps, const char* cache_path) {

@@ -105,6 +105,21 @@ constexpr uint32_t kErrBarrierTimeout = 2u;
 // kPullUnit consecutive entries [o0, o0 + kPullUnit) of one projection's ELL.
 struct PullUnit { uint32_t proj, o0; };
 
+// One plastic projection (STDP).  Per ELL cell: the plasticity value and the
+// weight it scales (w x 2^S, FP32); per post cell: where its teacher's spike
+// sits above the step's history base (~0u: none).
+struct PlastDev {
+  uint32_t proj;                  // index into projs
+  uint32_t rule;                  // SGB_STDP_HEBB / SGB_STDP_TEACHER
+  uint32_t window;                // pairing window (steps)
+  uint32_t pad_;
+  float a0, a1_i, a1_j, a2_ji, v_max, pad2_;
+  float* val;
+  const float* w0;
+  const uint32_t* teacher;
+  void* w_table;                  // the projection's ELL weights, rewritten each step
+};
+
 // Everything a step kernel needs, passed by value.
 struct StepArgs {
   Ctl* ctl;
@@ -120,6 +135,8 @@ struct StepArgs {
   const uint32_t* push_syn;
   const void* push_w;
   const PullUnit* pull_units;
+  const PlastDev* plast;          // [n_plast]
+  const PullUnit* stdp_units;     // {plastic projection, first ELL cell}
   float* su;                      // potential, or the refractory count (pack_u)
   float2* sg;                     // conductances of channels 0 and 1
   int* ring;                      // int2 per cell per slot, viewed as int[2]
@@ -135,6 +152,7 @@ struct StepArgs {
   uint32_t n_pad, n_words, n_segs, n_projs;
   uint32_t ring_slots, hist_rows;
   uint32_t n_upd_words, n_pull_units;
+  uint32_t n_plast, n_stdp_units;
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
   uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory
   uint32_t any_push;
@@ -156,6 +174,10 @@ int persistent_blocks_per_sm(bool bf16);
 // Dense pull (per-step driver): k_pull needs pull_setup() once per device
 // before its first launch.
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s);
+// STDP of the plastic projections (per-step drivers, between update and pull)
+// and the reset of their values to 1.
+cudaError_t launch_stdp(const StepArgs& a, int blocks, cudaStream_t s);
+cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t pull_setup();
 int pull_blocks_per_sm(const StepArgs& a);
 size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summary rows

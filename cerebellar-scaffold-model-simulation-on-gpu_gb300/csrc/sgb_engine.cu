@@ -58,6 +58,7 @@ Sim::~Sim() {
   if (d_ell) cudaFree(d_ell);
   if (d_push) cudaFree(d_push);
   if (d_misc) cudaFree(d_misc);
+  if (d_plast) cudaFree(d_plast);
   if (h_counts) cudaFreeHost(h_counts);
   if (h_raster) cudaFreeHost(h_raster);
   if (h_raster_off) cudaFreeHost(h_raster_off);
@@ -135,7 +136,8 @@ static float scaled_weight(float w, int32_t bits, bool bf16) {
 // units).  Entries are ell_entry words (at most 2^27 padded cells).
 static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, uint32_t n_pad,
                       uint32_t pad, bool bf16, ProjTables& t, std::vector<uint32_t>& syn,
-                      std::vector<float>& wf, std::vector<uint16_t>& wh) {
+                      std::vector<float>& wf, std::vector<uint16_t>& wh,
+                      std::vector<float>* w0 = nullptr, std::vector<uint32_t>* cell_of_syn = nullptr) {
   const size_t nnz = pr.pre_idx.size();
   std::vector<uint32_t> indeg((size_t)npost, 0);
   for (size_t i = 0; i < nnz; ++i) indeg[pr.post_idx[i]]++;
@@ -147,6 +149,8 @@ static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, ui
   if (cells >= (1ull << 32) - kPullUnit) return false;  // entry offsets are 32-bit
   syn.assign(align_up(cells, kPullUnit), pad);  // whole pull units
   if (bf16) wh.assign(cells, 0); else wf.assign(cells, 0.f);
+  if (w0) w0->assign(cells, 0.f);
+  if (cell_of_syn) cell_of_syn->assign(nnz, 0);
   // Each row sorted by (delay, pre, synapse): neighbouring entries then test
   // bits of one history row at nearby words.  The pulled sum is an integer,
   // so the order does not change it.
@@ -174,6 +178,8 @@ static bool build_ell(const Projection& pr, int32_t npost, uint32_t pre_base, ui
       syn[q] = ell_entry(pre_base + (uint32_t)pr.pre_idx[i], pr.delay[i], n_pad);
       const float w = scaled_weight(pr.weight[i], t.scale_bits, bf16);
       if (bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
+      if (w0) (*w0)[q] = ldexpf(pr.weight[i], t.scale_bits);
+      if (cell_of_syn) (*cell_of_syn)[i] = (uint32_t)q;
     }
   }
   return true;
@@ -331,6 +337,24 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   s.n_cells = first_id;
   s.ring_slots = (uint32_t)max_delay + 1;
   s.hist_rows = (uint32_t)max_delay;
+  // A plastic synapse with delay d reads its pre cell's spikes d .. d +
+  // window - 1 steps back, a teacher up to max_delay steps back.
+  bool any_plastic = false;
+  for (const Network& net : s.nets)
+    for (const Projection& pr : net.projs) {
+      if (!pr.plastic) continue;
+      any_plastic = true;
+      int dmax = 1;
+      for (uint8_t d : pr.delay) dmax = std::max(dmax, (int)d);
+      s.hist_rows = std::max<uint32_t>(
+          s.hist_rows, (uint32_t)std::max(max_delay + 1, dmax + pr.plast.window_steps));
+    }
+  if (any_plastic && cfg.exec_mode == SGB_EXEC_PERSISTENT)
+    return set_error(SGB_ERR_UNSUPPORTED,
+                     "plastic projections run with the graph or stream driver, not persistent");
+  if ((uint64_t)s.hist_rows * s.n_pad > 0xFFFFFFFFull)
+    return set_error(SGB_ERR_UNSUPPORTED, "spike history of %u steps x %u cells exceeds 2^32",
+                     s.hist_rows, s.n_pad);
 
   // ---- stimulus sources ----------------------------------------------------
   std::vector<uint32_t> src_mask(s.n_pad, 0);
@@ -361,6 +385,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   std::vector<std::vector<uint32_t>> ell_syn;
   std::vector<std::vector<float>> ell_wf;
   std::vector<std::vector<uint16_t>> ell_wh;
+  std::vector<std::vector<float>> plast_w0;  // per plastic projection: w x 2^S per ELL cell
   size_t pool = 0;
   const size_t wsz = s.bf16 ? 2 : 4;
   for (int32_t ni = 0; ni < n; ++ni) {
@@ -379,9 +404,18 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       ell_syn.emplace_back();
       ell_wf.emplace_back();
       ell_wh.emplace_back();
+      if (pr.plastic) {
+        PlastHost ph;
+        ph.net = ni;
+        ph.proj = (int32_t)pj;
+        ph.k = (uint32_t)s.projs.size();
+        s.plast.push_back(ph);
+        plast_w0.emplace_back();
+      }
       if (!build_ell(pr, net.pops[pr.post].num, s.segs[t.pre_seg].base, s.n_pad,
                      ell_pad(s.hist_rows, s.n_pad), s.bf16, t, ell_syn.back(), ell_wf.back(),
-                     ell_wh.back()))
+                     ell_wh.back(), pr.plastic ? &plast_w0.back() : nullptr,
+                     pr.plastic ? &s.plast.back().cell_of_syn : nullptr))
         return set_error(SGB_ERR_UNSUPPORTED, "projection %zu: dense table over 2^32 entries", pj);
       t.off_ell_syn = pool;
       pool = align_up(pool + ell_syn.back().size() * 4, 256);
@@ -539,6 +573,78 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       SGB_CUDA(l2_window_on(s, s.stream, true));
     }
   }
+  // ---- plastic projections: values, scaled weights, teachers, work units ----
+  if (!s.plast.empty()) {
+    std::vector<PlastDev> pd(s.plast.size());
+    std::vector<PullUnit> units;
+    size_t bytes = align_up(pd.size() * sizeof(PlastDev), 256);
+    const size_t off_units = bytes;
+    for (size_t i = 0; i < s.plast.size(); ++i) {
+      const ProjDev& P = s.projs[s.plast[i].k];
+      for (uint32_t o = 0; o < P.ell_n; o += kPullUnit) units.push_back({(uint32_t)i, o});
+    }
+    bytes = align_up(bytes + std::max<size_t>(units.size(), 1) * sizeof(PullUnit), 256);
+    std::vector<size_t> off_w0(s.plast.size()), off_t(s.plast.size());
+    for (size_t i = 0; i < s.plast.size(); ++i) {
+      PlastHost& ph = s.plast[i];
+      const ProjDev& P = s.projs[ph.k];
+      ph.cells = P.ell_n;
+      ph.off_val = bytes;
+      bytes = align_up(bytes + std::max<size_t>(ph.cells, 1) * 4, 256);
+      off_w0[i] = bytes;
+      bytes = align_up(bytes + std::max<size_t>(ph.cells, 1) * 4, 256);
+      off_t[i] = bytes;
+      bytes = align_up(bytes + std::max<size_t>(P.post_count, 1) * 4, 256);
+    }
+    SGB_CUDA(cudaMalloc(&s.d_plast, bytes));
+    char* pb = (char*)s.d_plast;
+    for (size_t i = 0; i < s.plast.size(); ++i) {
+      const PlastHost& ph = s.plast[i];
+      const ProjDev& P = s.projs[ph.k];
+      const Projection& pr = s.nets[ph.net].projs[ph.proj];
+      const sgb_plasticity_params& q = pr.plast;
+      // Teacher of each post cell: its synapse of the teacher projection with
+      // the lowest (delay, pre id); its spike sits `delay` rows above step t.
+      std::vector<uint32_t> teacher(P.post_count, 0xFFFFFFFFu);
+      if (q.rule == SGB_STDP_TEACHER) {
+        const Projection& tp = s.nets[ph.net].projs[q.teacher_proj];
+        const uint32_t tbase = s.segs[s.net_seg0[ph.net] + tp.pre].base;
+        std::vector<uint64_t> best(P.post_count, ~0ull);
+        for (size_t j = 0; j < tp.pre_idx.size(); ++j) {
+          const uint64_t key = ((uint64_t)tp.delay[j] << 32) | tp.pre_idx[j];
+          uint64_t& b = best[tp.post_idx[j]];
+          if (key < b) b = key;
+        }
+        for (uint32_t p = 0; p < P.post_count; ++p)
+          if (best[p] != ~0ull)
+            teacher[p] = (uint32_t)(best[p] >> 32) * s.n_pad + tbase + (uint32_t)(best[p] & 0xFFFFFFFFu);
+      }
+      SGB_CUDA(cudaMemcpy(pb + off_w0[i], plast_w0[i].data(), ph.cells * 4, cudaMemcpyHostToDevice));
+      SGB_CUDA(cudaMemcpy(pb + off_t[i], teacher.data(), (size_t)P.post_count * 4, cudaMemcpyHostToDevice));
+      PlastDev& d = pd[i];
+      memset(&d, 0, sizeof d);
+      d.proj = ph.k;
+      d.rule = (uint32_t)q.rule;
+      d.window = (uint32_t)q.window_steps;
+      d.a0 = q.a0;
+      d.a1_i = q.a1_i;
+      d.a1_j = q.a1_j;
+      d.a2_ji = q.a2_ji;
+      d.v_max = q.v_max;
+      d.val = (float*)(pb + ph.off_val);
+      d.w0 = (const float*)(pb + off_w0[i]);
+      d.teacher = (const uint32_t*)(pb + off_t[i]);
+      d.w_table = const_cast<void*>(P.ell_w);
+    }
+    std::vector<std::vector<float>>().swap(plast_w0);
+    SGB_CUDA(cudaMemcpy(pb, pd.data(), pd.size() * sizeof(PlastDev), cudaMemcpyHostToDevice));
+    if (!units.empty())
+      SGB_CUDA(cudaMemcpy(pb + off_units, units.data(), units.size() * sizeof(PullUnit), cudaMemcpyHostToDevice));
+    a.plast = (const PlastDev*)pb;
+    a.n_plast = (uint32_t)pd.size();
+    a.stdp_units = (const PullUnit*)(pb + off_units);
+    a.n_stdp_units = (uint32_t)units.size();
+  }
   SGB_CUDA(pull_setup());
   s.pull_blocks = pull_blocks_per_sm(a) * s.sm_count;
   const int bpsm = std::min(cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : 1,
@@ -590,6 +696,7 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
   SGB_CUDA(cudaMemsetAsync(a.ring, 0, (size_t)s.ring_slots * s.n_pad * 8, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.hist, 0, s.hist_bytes, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
+  if (a.n_plast) SGB_CUDA(launch_plast_reset(a, s.deliver_blocks, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.items, 0, (size_t)2 * a.item_cap * sizeof(uint2), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.totals, 0, s.segs.size() * sizeof(double), s.stream));
   SGB_CUDA(cudaStreamSynchronize(s.stream));
@@ -613,6 +720,10 @@ static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nla
   } else {
     for (uint32_t i = 0; i < c; ++i) {
       if ((e = launch_update(a, st))) return e;
+      if (a.n_plast) {
+        if ((e = launch_stdp(a, s.deliver_blocks, st))) return e;
+        L++;
+      }
       if (a.n_pull_units) {
         if ((e = launch_pull(a, s.pull_blocks, st))) return e;
         L++;
@@ -841,6 +952,8 @@ int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
   if (proj < 0 || proj >= (int32_t)s.nets[net].projs.size())
     return set_error(SGB_ERR_ARG, "projection %d out of range", proj);
   if (mode != SGB_PROP_CSR && mode != SGB_PROP_ELL) return set_error(SGB_ERR_ARG, "mode must be CSR or ELL");
+  if (s.nets[net].projs[proj].plastic && mode != SGB_PROP_ELL)
+    return set_error(SGB_ERR_UNSUPPORTED, "projection %d is plastic: it stays in dense pull", proj);
   s.projs[s.net_proj0[net] + proj].mode = (uint32_t)mode;
   return upload_modes(s);
 }
@@ -940,6 +1053,9 @@ static int apply_modes(Sim& s, const std::vector<int32_t>& modes) {
 }
 
 int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
+  if (!s.plast.empty())
+    return set_error(SGB_ERR_UNSUPPORTED,
+                     "handles with plastic projections keep their modes and driver (not tuned)");
   if (n_steps < 1) return set_error(SGB_ERR_ARG, "n_steps must be >= 1");
   const std::string sig = tune_signature(s);
   std::vector<int32_t> modes;
@@ -1064,6 +1180,10 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
       SGB_CUDA(cudaEventRecord(ev[0], s.stream));
       SGB_CUDA(launch_update(a, s.stream));
       SGB_CUDA(cudaEventRecord(ev[1], s.stream));
+      if (a.n_plast) {
+        SGB_CUDA(launch_stdp(a, s.deliver_blocks, s.stream));
+        s.launches++;
+      }
       SGB_CUDA(cudaEventRecord(ev[4], s.stream));
       SGB_CUDA(launch_pull(a, s.pull_blocks, s.stream));
       SGB_CUDA(cudaEventRecord(ev[5], s.stream));
@@ -1099,6 +1219,23 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
     if (launches) launches[k] = nl[k];
   }
   return SGB_OK;
+}
+
+}  // namespace sgb
+
+namespace sgb {
+
+int sim_plastic_values(Sim& s, int32_t net, int32_t proj, float* values) {
+  if (!values) return set_error(SGB_ERR_ARG, "values is NULL");
+  for (const PlastHost& ph : s.plast) {
+    if (ph.net != net || ph.proj != proj) continue;
+    std::vector<float> v(std::max<size_t>(ph.cells, 1));
+    SGB_CUDA(cudaStreamSynchronize(s.stream));
+    SGB_CUDA(cudaMemcpy(v.data(), (char*)s.d_plast + ph.off_val, ph.cells * 4, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < ph.cell_of_syn.size(); ++i) values[i] = v[ph.cell_of_syn[i]];
+    return SGB_OK;
+  }
+  return set_error(SGB_ERR_ARG, "projection %d of net %d is not plastic", proj, net);
 }
 
 }  // namespace sgb

@@ -21,6 +21,15 @@ struct ProjTables {
   size_t off_ell_syn = 0, off_ell_w = 0;  // offsets inside the ELL pool
 };
 
+// Host view of one plastic projection: the ELL cell of each synapse (in the
+// projection's synapse order), for reading the values back.
+struct PlastHost {
+  int32_t net = 0, proj = 0;
+  uint32_t k = 0;                 // index into projs
+  std::vector<uint32_t> cell_of_syn;
+  size_t off_val = 0, cells = 0;  // in d_plast
+};
+
 struct Sim {
   sgb_config cfg{};
   std::vector<Network> nets;
@@ -55,6 +64,9 @@ struct Sim {
   int pull_blocks = 0;        // k_pull grid (resident blocks per SM x SMs)
   size_t hist_bytes = 0;      // spike history + its summary
   int persistent_blocks = 0;
+  // Plasticity (STDP) of plastic projections.
+  void* d_plast = nullptr;
+  std::vector<PlastHost> plast;
   // Persisting L2 window over the cell state (su, sg).
   void* l2_base = nullptr;
   size_t l2_window = 0, l2_setaside = 0, l2_prev_limit = 0;
@@ -86,6 +98,7 @@ int sim_totals(Sim& s, double* totals);
 int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode);
 int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path);
 int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t* launches);
+int sim_plastic_values(Sim& s, int32_t net, int32_t proj, float* values);
 int sim_set_stream(Sim& s, cudaStream_t st);
 
 }  // namespace sgb

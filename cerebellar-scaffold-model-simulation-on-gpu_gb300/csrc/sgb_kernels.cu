@@ -547,6 +547,77 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
   if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
 }
 
+// STDP of the plastic projections, step t (SynapticPlasticity.cu:40-120), run
+// after the cells of step t updated and before the dense pull that delivers
+// into slot t + 1, so that delivery uses the new values -- in the reference
+// the propagation of the next millisecond follows invoke_stdp_plasticity.
+// One warp per unit of 1,024 ELL cells, one lane per cell.  The entry of a
+// cell is its pre cell's spike-bit offset for step t + 1 - d above the history
+// row of step t, so the spikes of steps t - d - s are at e + (s + 1) n_pad;
+// the post cell's spike of step t is at its own index, a teacher's at the
+// offset precomputed per post cell.  The history is read-only here.
+__device__ __forceinline__ uint32_t hist_bit(const uint32_t* hb, uint32_t off) {
+  return (__ldg(hb + (off >> 5)) >> (off & 31u)) & 1u;
+}
+
+template <bool BF16>
+__global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5, nw = (gridDim.x * kBlock) >> 5;
+  const StepIdx ix = step_of(a);
+  const uint32_t* hb = hist_base(a, ix.hrow);
+  const uint32_t pad = a.hist_rows * a.n_pad;
+  for (uint32_t u = gw; u < a.n_stdp_units; u += nw) {
+    const PullUnit un = a.stdp_units[u];
+    const PlastDev& L = a.plast[un.proj];
+    const ProjDev& P = a.projs[L.proj];
+    const uint32_t end = min(un.o0 + kPullUnit, P.ell_n);
+    for (uint32_t o = un.o0 + lane; o < end; o += 32u) {
+      const uint32_t e = __ldg(P.ell_syn + o);
+      if (e >= pad) continue;  // padding
+      const uint32_t post = P.ell_rowmajor ? o / P.ell_K : o % P.post_count;
+      const uint32_t so = L.rule == SGB_STDP_TEACHER ? __ldg(L.teacher + post) : P.post_base + post;
+      const bool s_post = so != 0xFFFFFFFFu && hist_bit(hb, so);
+      const bool s_pre = hist_bit(hb, e + a.n_pad) != 0u;
+      // Reference order: A0, A1_J (pre), A1_I (post / teacher), A2_JI window.
+      float dw = __fadd_rn(0.f, L.a0);
+      if (s_pre) dw = __fadd_rn(dw, L.a1_j);
+      if (s_post) dw = __fadd_rn(dw, L.a1_i);
+      if (s_post && L.a2_ji != 0.f)
+        for (uint32_t k = 0; k < L.window; ++k)
+          if (hist_bit(hb, e + (k + 1u) * a.n_pad)) dw = __fadd_rn(dw, L.a2_ji);
+      float v = __fadd_rn(L.val[o], dw);
+      v = v < 0.f ? 0.f : (v > L.v_max ? L.v_max : v);
+      L.val[o] = v;
+      const float tw = __fmul_rn(__ldg(L.w0 + o), v);
+      if (BF16)
+        reinterpret_cast<uint16_t*>(L.w_table)[o] = f32_to_bf16_bits(tw);
+      else
+        reinterpret_cast<float*>(L.w_table)[o] = tw;
+    }
+  }
+}
+
+// Plastic values back to 1 and the tables to the initial weights.
+template <bool BF16>
+__global__ void __launch_bounds__(kBlock) k_plast_reset(StepArgs a) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5, nw = (gridDim.x * kBlock) >> 5;
+  for (uint32_t u = gw; u < a.n_stdp_units; u += nw) {
+    const PullUnit un = a.stdp_units[u];
+    const PlastDev& L = a.plast[un.proj];
+    const uint32_t end = min(un.o0 + kPullUnit, a.projs[L.proj].ell_n);
+    for (uint32_t o = un.o0 + lane; o < end; o += 32u) {
+      L.val[o] = 1.f;
+      const float tw = __ldg(L.w0 + o);
+      if (BF16)
+        reinterpret_cast<uint16_t*>(L.w_table)[o] = f32_to_bf16_bits(tw);
+      else
+        reinterpret_cast<float*>(L.w_table)[o] = tw;
+    }
+  }
+}
+
 // Per-segment spike totals of the chunk, folded into the FP64 accumulators.
 __global__ void __launch_bounds__(kBlock) k_chunk_end(StepArgs a) {
   const uint32_t seg = blockIdx.x;
@@ -864,6 +935,24 @@ cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
     if (a.pull_sum) k_pull<false, true><<<blocks, kPullBlock, smem, s>>>(a);
     else k_pull<false, false><<<blocks, kPullBlock, smem, s>>>(a);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stdp(const StepArgs& a, int blocks, cudaStream_t s) {
+  if (!a.n_stdp_units) return cudaSuccess;
+  if (a.bf16)
+    k_stdp<true><<<blocks, kBlock, 0, s>>>(a);
+  else
+    k_stdp<false><<<blocks, kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s) {
+  if (!a.n_stdp_units) return cudaSuccess;
+  if (a.bf16)
+    k_plast_reset<true><<<blocks, kBlock, 0, s>>>(a);
+  else
+    k_plast_reset<false><<<blocks, kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 

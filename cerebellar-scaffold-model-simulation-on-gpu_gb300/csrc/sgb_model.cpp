@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <numeric>
 
 #include "sgb_philox.h"
@@ -349,6 +350,40 @@ int write_projection_dat(const Network& net, int32_t proj, const char* path) {
 
 // ---------------------------------------------------------------------------
 // Accumulator scales (see header).
+// Plastic values stay in [0, v_max] with v_max <= 1, so a plastic synapse
+// never delivers more than its initial weight and the accumulator scales
+// need no headroom.
+int add_plasticity(Network& net, int32_t proj, const sgb_plasticity_params* p) {
+  if (!p) return set_error(SGB_ERR_ARG, "params is NULL");
+  if (proj < 0 || proj >= (int32_t)net.projs.size())
+    return set_error(SGB_ERR_ARG, "projection %d out of range", proj);
+  Projection& pr = net.projs[proj];
+  if (pr.plastic) return set_error(SGB_ERR_ARG, "projection %d is already plastic", proj);
+  if (p->rule != SGB_STDP_HEBB && p->rule != SGB_STDP_TEACHER)
+    return set_error(SGB_ERR_ARG, "unknown plasticity rule %d", p->rule);
+  if (p->window_steps < 0 || p->window_steps > kMaxStdpWindow)
+    return set_error(SGB_ERR_RANGE, "window of %d steps not in 0..%d", p->window_steps,
+                     kMaxStdpWindow);
+  if (!(p->v_max > 0.f && p->v_max <= 1.f))
+    return set_error(SGB_ERR_RANGE, "v_max %g not in (0, 1]", (double)p->v_max);
+  if (!std::isfinite(p->a0) || !std::isfinite(p->a1_i) || !std::isfinite(p->a1_j) ||
+      !std::isfinite(p->a2_ji))
+    return set_error(SGB_ERR_ARG, "coefficients must be finite");
+  if (p->rule == SGB_STDP_TEACHER) {
+    if (p->teacher_proj < 0 || p->teacher_proj >= (int32_t)net.projs.size() ||
+        p->teacher_proj == proj)
+      return set_error(SGB_ERR_ARG, "teacher projection %d out of range", p->teacher_proj);
+    if (net.projs[p->teacher_proj].post != pr.post)
+      return set_error(SGB_ERR_ARG, "teacher projection %d does not target population %d",
+                       p->teacher_proj, pr.post);
+  }
+  pr.plastic = true;
+  pr.plast = *p;
+  if (p->rule == SGB_STDP_HEBB) pr.plast.teacher_proj = -1;
+  pr.mode = SGB_PROP_ELL;
+  return SGB_OK;
+}
+
 void accumulator_scale_bits(const Network& net, bool bf16, std::vector<int32_t>& bits) {
   const size_t np = net.pops.size();
   bits.assign(np * 2, kMaxScaleBits);

@@ -33,6 +33,8 @@ struct Projection {
   std::vector<uint32_t> pre_idx, post_idx;  // population-local ids
   std::vector<float> weight;                // magnitude added to the accumulator
   std::vector<uint8_t> delay;               // exchange steps, 1..kMaxDelay
+  bool plastic = false;                     // STDP (add_plasticity)
+  sgb_plasticity_params plast{};
 };
 
 struct InputSource {
@@ -69,6 +71,8 @@ int add_input(Network& net, int32_t pop, int64_t n_ids, const uint32_t* ids,
 int load_input_dat(Network& net, const char* path, int32_t pop, const sgb_input_params* params,
                    int32_t* src_id);
 int write_projection_dat(const Network& net, int32_t proj, const char* path);
+int add_plasticity(Network& net, int32_t proj, const sgb_plasticity_params* params);
+constexpr int kMaxStdpWindow = 64;  // longest pairing window (steps)
 int build_scaffold(Network& net, int32_t config, double scale, uint64_t seed);
 
 // Fixed-point fraction bits of each (population, accumulator) pair: the

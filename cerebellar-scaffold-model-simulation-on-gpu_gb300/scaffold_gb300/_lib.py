@@ -19,6 +19,7 @@ ERRORS = {
 NORMAL, INPUT, OUTPUT = 0, 1, 2
 CH_EXC, CH_INH = 0, 1
 PROP_AUTO, PROP_CSR, PROP_ELL = 0, 1, 2
+STDP_HEBB, STDP_TEACHER = 0, 1
 WEIGHT_FP32, WEIGHT_BF16 = 0, 1
 EXEC_GRAPH, EXEC_PERSISTENT, EXEC_STREAM = 0, 1, 2
 INPUT_POISSON, INPUT_PERIODIC = 0, 1
@@ -44,6 +45,12 @@ class InputParams(C.Structure):
     _fields_ = [("kind", C.c_int32), ("rate_hz", C.c_float), ("phase_ms", C.c_double),
                 ("win_period_ms", C.c_double), ("win_start_ms", C.c_double),
                 ("win_end_ms", C.c_double)]
+
+
+class PlasticityParams(C.Structure):
+    _fields_ = [("rule", C.c_int32), ("teacher_proj", C.c_int32), ("window_steps", C.c_int32),
+                ("a0", C.c_float), ("a1_i", C.c_float), ("a1_j", C.c_float), ("a2_ji", C.c_float),
+                ("v_max", C.c_float)]
 
 
 class PopulationInfo(C.Structure):
@@ -112,6 +119,9 @@ PROTOTYPES = {
     "sgb_net_input_info": (C.c_int, [vp, i32, P(InputInfo)]),
     "sgb_net_input_ids": (C.c_int, [vp, i32, u32p]),
     "sgb_net_write_projection_dat": (C.c_int, [vp, i32, C.c_char_p]),
+    "sgb_net_add_plasticity": (C.c_int, [vp, i32, P(PlasticityParams)]),
+    "sgb_net_plasticity_info": (C.c_int, [vp, i32, i32p, P(PlasticityParams)]),
+    "sgb_sim_plastic_values": (C.c_int, [vp, i32, i32, f32p]),
     "sgb_sim_create": (C.c_int, [P(Config), P(vp), P(C.c_uint64), i32, P(vp)]),
     "sgb_sim_destroy": (None, [vp]),
     "sgb_sim_set_stream": (C.c_int, [vp, vp]),

@@ -213,6 +213,24 @@ class Network:
     def write_projection_dat(self, proj: int, path: str) -> None:
         L.check(L.lib().sgb_net_write_projection_dat(self._h, proj, path.encode()))
 
+    def add_plasticity(self, proj: int, rule: int = L.STDP_HEBB, *, teacher: int = -1,
+                       window: int = 50, a0: float = 0.0, a1_i: float = 0.0, a1_j: float = 0.0,
+                       a2_ji: float = 0.0, v_max: float = 1.0) -> None:
+        """STDP on projection `proj` (the reference's Hebb / Teacher rules,
+        SynapticPlasticity.cu:40-120, with constant coefficients)."""
+        p = L.PlasticityParams(rule, teacher, window, a0, a1_i, a1_j, a2_ji, v_max)
+        L.check(L.lib().sgb_net_add_plasticity(self._h, proj, C.byref(p)))
+
+    def plasticity(self, proj: int):
+        """Plasticity parameters of projection `proj` as a dict, or None."""
+        flag = C.c_int32()
+        p = L.PlasticityParams()
+        L.check(L.lib().sgb_net_plasticity_info(self._h, proj, C.byref(flag), C.byref(p)))
+        if not flag.value:
+            return None
+        return dict(rule=p.rule, teacher=p.teacher_proj, window=p.window_steps, a0=p.a0,
+                    a1_i=p.a1_i, a1_j=p.a1_j, a2_ji=p.a2_ji, v_max=p.v_max)
+
 
 class Simulation:
     """Device simulation of one or more independent networks (instances)."""
@@ -361,6 +379,13 @@ class Simulation:
         t = np.zeros(self.n_segments, np.float64)
         L.check(L.lib().sgb_sim_spike_totals(self._h, _ptr(t, C.c_double)))
         return t
+
+    def plastic_values(self, net: int, proj: int) -> np.ndarray:
+        """Plasticity values of a plastic projection's synapses (synapse order)."""
+        n = self.nets[net].synapses(proj)[0].size
+        v = np.empty(max(n, 1), np.float32)
+        L.check(L.lib().sgb_sim_plastic_values(self._h, net, proj, _ptr(v, C.c_float)))
+        return v[:n]
 
     def set_propagation(self, net: int, proj: int, mode: int) -> None:
         L.check(L.lib().sgb_sim_set_propagation(self._h, net, proj, mode))

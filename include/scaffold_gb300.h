@@ -102,6 +102,31 @@ typedef struct sgb_input_params {
   double win_end_ms;
 } sgb_input_params;
 
+/* Synaptic plasticity of one projection: the reference's STDP rules
+ * (SynapticPlasticity.cu:40-120, invoke_stdp_plasticity :123-140; compiled
+ * in but switched off there, NumOfPlasticity = 0, struct_enum_def.h:50-53).
+ * Every synapse carries a value v (1 at start) that scales its weight; each
+ * step, after the cells update, every synapse of the projection adds
+ *   a0 + a1_j [pre spiked at t - d] + a1_i [post (Hebb) / teacher spiked]
+ *      + a2_ji [post / teacher spiked] * #{s < window : pre spiked at t - d - s}
+ * (in that order, FP32) and is clamped to [0, v_max]; the delivery of the
+ * next step uses the new value.  Teacher: the teacher of a post cell is the
+ * first synapse of `teacher_proj` onto it (lowest delay, then lowest pre id;
+ * the reference takes the first ELL entry, :89, of a single-delay
+ * projection), its spike read at t - its delay.  The reference's
+ * coefficients are functions of (v, s); the ones it defines are constants
+ * (:8-17), which is what these are. */
+#define SGB_STDP_HEBB 0
+#define SGB_STDP_TEACHER 1
+typedef struct sgb_plasticity_params {
+  int32_t rule;          /* SGB_STDP_HEBB or SGB_STDP_TEACHER                          */
+  int32_t teacher_proj;  /* Teacher: projection onto the same post population       */
+  int32_t window_steps;  /* pairing window of the a2_ji term (reference: 50), 0..64  */
+  float a0, a1_i, a1_j, a2_ji;
+  float v_max;           /* upper clamp, 0 < v_max <= 1 (reference Hebb: 1; Teacher has */
+                         /* none, and its only coefficient depresses)                   */
+} sgb_plasticity_params;
+
 typedef struct sgb_population_info {
   int32_t num, dev_type, c_num, n_in_projections;
   float Cm, El, dt_ref, Ie, Vr, Vth, gL;
@@ -232,6 +257,13 @@ int sgb_net_counts(const sgb_net* net, int32_t* n_pops, int32_t* n_projs, int32_
                    int64_t* n_neurons, int64_t* n_synapses);
 int sgb_net_population_info(const sgb_net* net, int32_t pop, sgb_population_info* info);
 int sgb_net_projection_info(const sgb_net* net, int32_t proj, sgb_projection_info* info);
+/* Makes projection `proj` plastic (replaces the reference's Init_Plasticity,
+ * SynapticPlasticity.cu:20-34).  A plastic projection is delivered by dense
+ * pull (its weights change every step) and needs the graph or stream driver. */
+int sgb_net_add_plasticity(sgb_net* net, int32_t proj, const sgb_plasticity_params* params);
+/* *plastic = 1 and the parameters when projection `proj` is plastic, else 0. */
+int sgb_net_plasticity_info(const sgb_net* net, int32_t proj, int32_t* plastic,
+                            sgb_plasticity_params* params);
 /* Copies the synapse arrays of a projection (any pointer may be NULL). */
 int sgb_net_projection_synapses(const sgb_net* net, int32_t proj, uint32_t* pre, uint32_t* post,
                                 float* weight, uint8_t* delay);
@@ -310,6 +342,10 @@ int sgb_sim_spike_totals(sgb_sim* sim, double* totals);
 /* Propagation mode of projection `proj` of net `net` (SGB_PROP_CSR/ELL). */
 int sgb_sim_set_propagation(sgb_sim* sim, int32_t net, int32_t proj, int32_t mode);
 int sgb_sim_get_propagation(const sgb_sim* sim, int32_t net, int32_t proj, int32_t* mode);
+
+/* Current plasticity values v of the synapses of plastic projection `proj`
+ * of net `net`, in the projection's synapse order (sgb_net_projection_synapses). */
+int sgb_sim_plastic_values(sgb_sim* sim, int32_t net, int32_t proj, float* values);
 
 /* Autotuner: times the CSR and ELL propagation of every projection over
  * `n_steps` steps of the running simulation (restoring its state afterwards)

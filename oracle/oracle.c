@@ -87,8 +87,22 @@ typedef struct {
   double* wd;       /* FP64 mode */
 } push_rows;
 
+/* One plastic projection. */
+typedef struct {
+  const orc_plast* p;
+  float* v32;         /* per synapse */
+  double* v64;
+  float* w0;          /* w * 2^S per synapse (FP32 mode) */
+  int64_t* teacher;   /* per post: global id of the teacher cell, -1 none */
+  int32_t* tdelay;    /* per post: delay of the teacher synapse */
+} plast_state;
+
 struct orc_sim {
   orc_net net;
+  plast_state* pl;          /* [n_plast] */
+  int32_t* plast_of;        /* [n_projs]: index into pl or -1 */
+  uint8_t* hist;            /* [H][n_cells] spikes, row = step % H */
+  int32_t H;
   int64_t n_cells;
   int64_t* base;            /* [n_pops] first global id */
   int32_t D;                /* ring slots */
@@ -181,6 +195,51 @@ int orc_create(const orc_net* net, orc_sim** out) {
   s->ring_fix = (int32_t*)calloc((size_t)s->D * N * 2, 4);
   s->ring_d = (double*)calloc((size_t)s->D * N * 2, 8);
   s->spk = (uint8_t*)calloc((size_t)N, 1);
+  /* Plasticity: values start at 1; history deep enough for the window. */
+  s->plast_of = (int32_t*)malloc((size_t)(net->n_projs > 0 ? net->n_projs : 1) * 4);
+  for (int i = 0; i < net->n_projs; ++i) s->plast_of[i] = -1;
+  s->pl = (plast_state*)calloc((size_t)(net->n_plast > 0 ? net->n_plast : 1), sizeof(plast_state));
+  s->H = 0;
+  for (int k = 0; k < net->n_plast; ++k) {
+    const orc_plast* pp = &net->plast[k];
+    const orc_proj* p = &net->projs[pp->proj];
+    plast_state* ps = &s->pl[k];
+    s->plast_of[pp->proj] = k;
+    ps->p = pp;
+    const int64_t m = p->n > 0 ? p->n : 1;
+    ps->v32 = (float*)malloc((size_t)m * 4);
+    ps->v64 = (double*)malloc((size_t)m * 8);
+    ps->w0 = (float*)malloc((size_t)m * 4);
+    const float scale = ldexpf(1.0f, s->scale_bits[p->post * 2 + p->channel]);
+    int dmax = 1;
+    for (int64_t q = 0; q < p->n; ++q) {
+      ps->v32[q] = 1.0f;
+      ps->v64[q] = 1.0;
+      ps->w0[q] = p->weight[q] * scale; /* power of two: exact */
+      if (p->delay[q] > dmax) dmax = p->delay[q];
+    }
+    const int need = (maxd + 1 > dmax + pp->window) ? maxd + 1 : dmax + pp->window;
+    if (need > s->H) s->H = need;
+    const int64_t npost = net->pops[p->post].num > 0 ? net->pops[p->post].num : 1;
+    ps->teacher = (int64_t*)malloc((size_t)npost * 8);
+    ps->tdelay = (int32_t*)calloc((size_t)npost, 4);
+    for (int64_t j = 0; j < npost; ++j) ps->teacher[j] = -1;
+    if (pp->rule == 1) {
+      /* teacher of a post: its teacher synapse of lowest (delay, pre id) */
+      const orc_proj* tp = &net->projs[pp->teacher_proj];
+      for (int64_t q = 0; q < tp->n; ++q) {
+        const uint32_t j = tp->post_idx[q];
+        const int64_t g = s->base[tp->pre] + tp->pre_idx[q];
+        const int32_t d = tp->delay[q];
+        if (ps->teacher[j] < 0 || d < ps->tdelay[j] ||
+            (d == ps->tdelay[j] && g < ps->teacher[j])) {
+          ps->teacher[j] = g;
+          ps->tdelay[j] = d;
+        }
+      }
+    }
+  }
+  s->hist = s->H ? (uint8_t*)calloc((size_t)s->H * N, 1) : NULL;
   /* u0 = Vr + (Vth - Vr) * U(0,1] (init_params.cu:346); id = global index. */
   for (int p = 0; p < np; ++p) {
     const orc_pop* P = &net->pops[p];
@@ -207,6 +266,11 @@ void orc_destroy(orc_sim* s) {
   free(s->rows); free(s->base); free(s->scale_bits); free(s->src_mask); free(s->thresh);
   free(s->rates); free(s->u32); free(s->g32); free(s->u64); free(s->g64); free(s->ref);
   free(s->ring_fix); free(s->ring_d); free(s->spk);
+  for (int k = 0; k < s->net.n_plast; ++k) {
+    free(s->pl[k].v32); free(s->pl[k].v64); free(s->pl[k].w0);
+    free(s->pl[k].teacher); free(s->pl[k].tdelay);
+  }
+  free(s->pl); free(s->plast_of); free(s->hist);
   free(s);
 }
 
@@ -331,6 +395,64 @@ static int lif64(const orc_pop* P, const lif_k* k, int substeps, double* u_, dou
   return spk;
 }
 
+/* ---- plasticity ------------------------------------------------------------ */
+/* Spike of global cell g at step `step` (no spikes before step 0). */
+static int spiked(const orc_sim* s, int64_t g, int64_t step) {
+  if (step < 0) return 0;
+  return s->hist[(step % s->H) * s->n_cells + g];
+}
+
+/* One step of Hebb_plasticity / Teacher_plasticity (SynapticPlasticity.cu:
+ * 40-75, 78-120) over every synapse of the projection: dw = A0 + A1_J [pre
+ * at t - d] + A1_I [post at t / teacher at t - its delay] + A2_JI x #window
+ * pre spikes at t - d - s, summed in that order; v = clamp(v + dw). */
+static void stdp_step(orc_sim* s, plast_state* ps, uint64_t t) {
+  const orc_plast* pp = ps->p;
+  const orc_proj* pr = &s->net.projs[pp->proj];
+  const int fp64 = s->net.mode == ORC_FP64;
+  const int64_t tt = (int64_t)t;
+  for (int64_t q = 0; q < pr->n; ++q) {
+    const int64_t pre_g = s->base[pr->pre] + pr->pre_idx[q];
+    const int64_t d = pr->delay[q];
+    const uint32_t j = pr->post_idx[q];
+    int s_post;
+    if (pp->rule == 0)
+      s_post = s->spk[s->base[pr->post] + j];
+    else
+      s_post = ps->teacher[j] >= 0 && spiked(s, ps->teacher[j], tt - ps->tdelay[j]);
+    const int s_pre = spiked(s, pre_g, tt - d);
+    int nwin = 0;
+    if (s_post && pp->a2_ji != 0.0f)
+      for (int k = 0; k < pp->window; ++k) nwin += spiked(s, pre_g, tt - d - k);
+    if (!fp64) {
+      float dw = 0.0f + pp->a0;
+      if (s_pre) dw = dw + pp->a1_j;
+      if (s_post) dw = dw + pp->a1_i;
+      for (int k = 0; k < nwin; ++k) dw = dw + pp->a2_ji;
+      float v = ps->v32[q] + dw;
+      v = v < 0.0f ? 0.0f : (v > pp->v_max ? pp->v_max : v);
+      ps->v32[q] = v;
+    } else {
+      double dw = 0.0 + (double)pp->a0;
+      if (s_pre) dw += (double)pp->a1_j;
+      if (s_post) dw += (double)pp->a1_i;
+      dw += (double)nwin * (double)pp->a2_ji;
+      double v = ps->v64[q] + dw;
+      v = v < 0.0 ? 0.0 : (v > (double)pp->v_max ? (double)pp->v_max : v);
+      ps->v64[q] = v;
+    }
+  }
+}
+
+int orc_plastic_values(const orc_sim* s, int32_t proj, float* values) {
+  if (proj < 0 || proj >= s->net.n_projs || s->plast_of[proj] < 0) return -1;
+  const plast_state* ps = &s->pl[s->plast_of[proj]];
+  const orc_proj* pr = &s->net.projs[proj];
+  for (int64_t q = 0; q < pr->n; ++q)
+    values[q] = s->net.mode == ORC_FP64 ? (float)ps->v64[q] : ps->v32[q];
+  return 0;
+}
+
 int orc_run(orc_sim* s, int64_t n_steps, uint32_t* counts, uint32_t* raster, int64_t raster_cap,
             int64_t* raster_off) {
   const orc_net* n = &s->net;
@@ -375,7 +497,26 @@ int orc_run(orc_sim* s, int64_t n_steps, uint32_t* counts, uint32_t* raster, int
       if (counts) counts[step * n->n_pops + p] = cnt;
     }
     if (raster_off) raster_off[step + 1] = rfill;
-    /* 2. delivery of step t's spikes into the accumulators of t + delay */
+    if (s->H) memcpy(&s->hist[(int64_t)(t % (uint64_t)s->H) * N], s->spk, (size_t)N);
+    /* 2. plasticity of step t, then delivery of plastic projections on
+     * arrival: spikes of step t + 1 - d into the accumulators of t + 1 */
+    for (int k = 0; k < n->n_plast; ++k) stdp_step(s, &s->pl[k], t);
+    for (int k = 0; k < n->n_plast; ++k) {
+      const plast_state* ps = &s->pl[k];
+      const orc_proj* pr = &n->projs[ps->p->proj];
+      const int64_t sl = (int64_t)((t + 1) % (uint64_t)s->D);
+      for (int64_t q = 0; q < pr->n; ++q) {
+        const int64_t pre_g = s->base[pr->pre] + pr->pre_idx[q];
+        if (!spiked(s, pre_g, (int64_t)t + 1 - pr->delay[q])) continue;
+        const int64_t at = (sl * N + s->base[pr->post] + pr->post_idx[q]) * 2 + pr->channel;
+        if (fp64)
+          s->ring_d[at] += (double)pr->weight[q] * ps->v64[q];
+        else
+          s->ring_fix[at] += (int32_t)rintf(table_w(n, ps->w0[q] * ps->v32[q]));
+      }
+    }
+    /* 3. delivery of step t's spikes into the accumulators of t + delay
+     * (plastic projections: counted here, delivered above) */
     for (int i = 0; i < n->n_projs; ++i) {
       const orc_proj* pr = &n->projs[i];
       const push_rows* r = &s->rows[i];
@@ -383,6 +524,7 @@ int orc_run(orc_sim* s, int64_t n_steps, uint32_t* counts, uint32_t* raster, int
       for (int64_t j = 0; j < n->pops[pr->pre].num; ++j) {
         if (!s->spk[pre0 + j]) continue;
         s->events += r->row[j + 1] - r->row[j];
+        if (s->plast_of[i] >= 0) continue;
         for (int64_t q = r->row[j]; q < r->row[j + 1]; ++q) {
           const int64_t sl = (int64_t)((t + r->delay[q]) % (uint64_t)s->D);
           const int64_t at = (sl * N + post0 + r->post[q]) * 2 + pr->channel;

@@ -14,7 +14,14 @@
  *   propagation   spike_propagation / host_spike_propagation
  *                 (Simulation_header.cu:83-101, 468-493) with per-synapse
  *                 delays, restated as delivery of each spike into the
- *                 accumulator of step t + delay.
+ *                 accumulator of step t + delay;
+ *   plasticity    Hebb_plasticity / Teacher_plasticity (SynapticPlasticity.cu:
+ *                 40-120), applied after the cells of step t; a plastic
+ *                 projection is delivered on arrival (the spike of step
+ *                 t + 1 - d into the accumulator of t + 1, after step t's
+ *                 plasticity), as the reference reads it d steps late.
+ *                 The reference has this code switched off and no test of
+ *                 it: this part of the oracle is unpinned.
  * Two arithmetic modes:
  *   ORC_FP32  the FP32 formulation of the CUDA kernels, one rounding per
  *             operation (compiled with -ffp-contract=off), fixed-point
@@ -58,6 +65,13 @@ typedef struct orc_src {
   const uint32_t* ids;
 } orc_src;
 
+/* Plasticity of one projection (SynapticPlasticity.cu:40-120): rule 0 Hebb,
+ * 1 Teacher; constant coefficients; values clamped to [0, v_max]. */
+typedef struct orc_plast {
+  int32_t proj, rule, teacher_proj, window;
+  float a0, a1_i, a1_j, a2_ji, v_max, pad_;
+} orc_plast;
+
 typedef struct orc_net {
   int32_t n_pops, n_projs, n_srcs, substeps;
   const orc_pop* pops;
@@ -66,6 +80,8 @@ typedef struct orc_net {
   double dt_ms;
   uint64_t seed;
   int32_t bf16, mode;
+  int32_t n_plast, pad_;
+  const orc_plast* plast;
 } orc_net;
 
 typedef struct orc_sim orc_sim;
@@ -87,6 +103,9 @@ int orc_run(orc_sim* s, int64_t n_steps, uint32_t* counts, uint32_t* raster, int
 int orc_get_state(const orc_sim* s, float* u, float* g, int32_t* ref);
 int orc_set_state(orc_sim* s, const float* u, const float* g, const int32_t* ref);
 int64_t orc_events(const orc_sim* s);
+/* Plasticity values of plastic projection `proj` (the net's projection index),
+ * in its synapse order; -1 if it is not plastic. */
+int orc_plastic_values(const orc_sim* s, int32_t proj, float* values);
 /* Input-cell spike flags of step t (1 byte per cell in global-id order; LIF
  * cells are left untouched).  Does not advance the simulation. */
 int orc_input_flags(const orc_sim* s, uint64_t t, uint8_t* flags);

@@ -40,11 +40,19 @@ class Src(C.Structure):
                 ("n_ids", C.c_int64), ("ids", C.POINTER(C.c_uint32))]
 
 
+class Plast(C.Structure):
+    _fields_ = [("proj", C.c_int32), ("rule", C.c_int32), ("teacher_proj", C.c_int32),
+                ("window", C.c_int32), ("a0", C.c_float), ("a1_i", C.c_float),
+                ("a1_j", C.c_float), ("a2_ji", C.c_float), ("v_max", C.c_float),
+                ("pad_", C.c_float)]
+
+
 class Net(C.Structure):
     _fields_ = [("n_pops", C.c_int32), ("n_projs", C.c_int32), ("n_srcs", C.c_int32),
                 ("substeps", C.c_int32), ("pops", C.POINTER(Pop)), ("projs", C.POINTER(Proj)),
                 ("srcs", C.POINTER(Src)), ("dt_ms", C.c_double), ("seed", C.c_uint64),
-                ("bf16", C.c_int32), ("mode", C.c_int32)]
+                ("bf16", C.c_int32), ("mode", C.c_int32), ("n_plast", C.c_int32),
+                ("pad_", C.c_int32), ("plast", C.POINTER(Plast))]
 
 
 _lib = None
@@ -79,6 +87,8 @@ def lib():
                                     C.POINTER(C.c_int32)]
         L.orc_events.argtypes = [C.c_void_p]
         L.orc_events.restype = C.c_int64
+        L.orc_plastic_values.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]
+        L.orc_plastic_values.restype = C.c_int
         _lib = L
     return _lib
 
@@ -134,9 +144,15 @@ class Oracle:
             q.phase_ms, q.win_period_ms = s["phase_ms"], s["win_period_ms"]
             q.win_start_ms, q.win_end_ms = s["win_start_ms"], s["win_end_ms"]
             q.n_ids, q.ids = len(ids), _p(ids, C.c_uint32)
-        self._keep += [pops, projs, srcs]
+        plast_list = desc.get("plast", [])
+        plast = (Plast * max(1, len(plast_list)))()
+        for i, q in enumerate(plast_list):
+            plast[i] = Plast(q["proj"], q["rule"], q["teacher"], q["window"], q["a0"], q["a1_i"],
+                             q["a1_j"], q["a2_ji"], q["v_max"], 0.0)
+        self._keep += [pops, projs, srcs, plast]
+        self.n_syn = [len(p["pre_idx"]) for p in desc["projs"]]
         self.net = Net(len(desc["pops"]), len(desc["projs"]), len(desc["srcs"]), substeps, pops,
-                       projs, srcs, dt_ms, seed, int(bf16), mode)
+                       projs, srcs, dt_ms, seed, int(bf16), mode, len(plast_list), 0, plast)
         self.n_pops = len(desc["pops"])
         self.n_cells = sum(p["num"] for p in desc["pops"])
         h = C.c_void_p()
@@ -191,6 +207,12 @@ class Oracle:
     def events(self):
         return lib().orc_events(self._h)
 
+    def plastic_values(self, proj):
+        v = np.empty(max(self.n_syn[proj], 1), np.float32)
+        if lib().orc_plastic_values(self._h, proj, _p(v, C.c_float)):
+            raise RuntimeError(f"projection {proj} is not plastic")
+        return v[: self.n_syn[proj]]
+
 
 def describe(net) -> dict:
     """Raw description of a scaffold_gb300.Network for the oracle."""
@@ -206,7 +228,12 @@ def describe(net) -> dict:
     srcs = []
     for pop, prm, ids in net.inputs():
         srcs.append(dict(pop=pop, ids=ids, **prm))
-    return dict(pops=pops, projs=projs, srcs=srcs)
+    plast = []
+    for pr in net.projections:
+        q = net.plasticity(pr.index)
+        if q is not None:
+            plast.append(dict(proj=pr.index, **q))
+    return dict(pops=pops, projs=projs, srcs=srcs, plast=plast)
 
 
 REF_DIR = os.path.join(HERE, "_ref")
