@@ -53,7 +53,8 @@ def parse():
                     help="exchange steps of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--exec", default="persistent", choices=["persistent", "graph"])
-    ap.add_argument("--no-ell-roofline", action="store_true")
+    ap.add_argument("--no-ell-roofline", action="store_true",
+                    help="skip the dense-pull and plasticity side measurements")
     ap.add_argument("--blocks-per-sm", type=int, default=1)
     ap.add_argument("--no-l2-persist", action="store_true",
                     help="plain L2 caching of the cell state (no persisting window)")
@@ -183,24 +184,67 @@ def cpu_baseline(wl: dict, sample_steps: int):
                       f"OpenMP over post cells"}
 
 
-def stream_read_gbs(nbytes: int, reps: int = 20) -> float:
-    """Read bandwidth of a plain device reduction (torch sum) over a buffer of
-    the same size: what streaming alone reaches for a launch of this size."""
+def stream_copy_gbs(nbytes: int, reps: int = 20) -> float:
+    """Bandwidth (read + write bytes) of a plain device copy of a buffer of
+    `nbytes`: the measured-peak method at this launch size."""
     import torch
 
     x = torch.ones(nbytes // 4, dtype=torch.int32, device="cuda")
+    y = torch.empty_like(x)
     for _ in range(3):
-        x.sum()
+        y.copy_(x)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record()
     for _ in range(reps):
-        x.sum()
+        y.copy_(x)
     e1.record()
     torch.cuda.synchronize()
-    gbs = nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
-    del x
+    gbs = 2 * nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del x, y
     return gbs
+
+
+def plasticity_leg(peak: float, bench_steps: int = 5, chunk: int = 1000):
+    """Config 2 with STDP on the parallel-fibre -> Purkinje projection (1.75M
+    synapses): the Teacher rule with the reference's depressing coefficient
+    (-0.01 per pre spike in a 50-step window before a teacher spike,
+    SynapticPlasticity.cu:13-18), basket cells standing in for the climbing
+    fibre (config 2 has no inferior olive).  Graph driver (plastic projections
+    are delivered by dense pull).  Realtime factor over `bench_steps` chunks and
+    the STDP kernel's per-launch time and algorithmic bytes (per updated
+    plastic synapse 16 B + W; with this rule only the rows of Purkinje cells
+    whose teacher fired are updated)."""
+    import torch
+
+    import scaffold_gb300 as sg
+
+    net = sg.scaffold(2, 1.0, 1)
+    names = {p.name: p.index for p in net.projections}
+    net.add_plasticity(names["granule_to_purkinje"], sg.STDP_TEACHER,
+                       teacher=names["basket_to_purkinje"], window=50, a2_ji=-0.01)
+    sim = sg.Simulation([net], [1], chunk_steps=chunk, exec_mode=sg.EXEC_GRAPH)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.run(chunk)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(bench_steps):
+        sim.enqueue(chunk)
+    e1.record(stream)
+    sim.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    mean_us, bytes_pl, nl = sim.profile(200)
+    sim.close()
+    gbs = bytes_pl[3] / (mean_us[3] * 1e-6) / 1e9 if mean_us[3] > 0 else 0.0
+    return {"workload": "config 2, FP32, Teacher STDP on granule_to_purkinje (1,750,000 synapses)",
+            "realtime_factor": bench_steps * chunk * 1e-4 / (ms * 1e-3),
+            "us_per_step": 1000.0 * ms / (bench_steps * chunk),
+            "k_stdp_us": mean_us[3], "k_stdp_bytes": bytes_pl[3], "k_stdp_gbs": gbs,
+            "k_stdp_frac": gbs / peak, "k_pull_us": mean_us[2], "k_update_us": mean_us[0],
+            "k_deliver_us": mean_us[1]}
 
 
 def ell_roofline(peak: float):
@@ -223,7 +267,7 @@ def ell_roofline(peak: float):
     info = sim.info()
     sim.close()
     gbs = bytes_pl[2] / (mean_us[2] * 1e-6) / 1e9
-    ceiling = stream_read_gbs(int(info.pull_entries) * 4)
+    ceiling = stream_copy_gbs(int(info.pull_entries) * 4)
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
@@ -235,7 +279,7 @@ def ell_roofline(peak: float):
             f"config 5: 4 seeds, {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
             "mean_us": mean_us[2], "bytes_per_launch": bytes_pl[2], "achieved": gbs,
             "unit": "GB/s", "peak": peak, "frac": gbs / peak,
-            "stream_read_gbs_same_bytes": ceiling,
+            "copy_gbs_same_bytes": ceiling,
             "l2": "entries 437 MB per launch (not L2-resident); no flush between launches"}
 
 
@@ -402,9 +446,11 @@ def run_gb300(a):
     mean_us, bytes_pl, nl = sim.profile(1000)
     phases = {n: {"mean_us": m, "bytes_per_launch": b,
                   "achieved_gbs": (b / (m * 1e-6) / 1e9) if m > 0 else 0.0}
-              for n, m, b, c in zip(["k_update", "k_deliver", "k_pull"], mean_us, bytes_pl, nl)
+              for n, m, b, c in zip(["k_update", "k_deliver", "k_pull", "k_stdp"], mean_us, bytes_pl,
+                                    nl)
               if c > 0}
     ell = None if a.no_ell_roofline else ell_roofline(peak)
+    plast = None if a.no_ell_roofline else plasticity_leg(peak)
     cpu = None
     if not a.no_cpu_baseline:
         try:
@@ -437,6 +483,7 @@ def run_gb300(a):
         "roofline": roof,
         "phase_profile": phases,
         "dense_ell_roofline": ell,
+        "plasticity": plast,
         "cpu_baseline": cpu,
         "clocks": clk,
     }

@@ -31,6 +31,7 @@ constexpr int kBlock = 256;           // threads per block of the per-step kerne
 constexpr int kPersistBlock = 1024;   // threads per block of the persistent kernel
 constexpr uint32_t kPushChunk = 256;  // synapses per push work item (8 per lane)
 constexpr uint32_t kPullUnit = 1024;  // ELL entries per dense-pull work unit (32 per lane)
+constexpr uint32_t kStdpUnit = 128;   // ELL cells per plasticity work unit (4 per lane)
 constexpr int kPullBlock = 1024;             // threads per k_pull block (one per SM)
 constexpr size_t kPullSumMax = 192 * 1024;  // largest spike summary k_pull stages (H rows)
 constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-major layout
@@ -97,6 +98,7 @@ struct Ctl {
   unsigned long long events;      // synaptic events (spikes x out-degree) since reset
   unsigned long long delivered;   // synapses walked by the CSR push since reset
   unsigned long long pulled;      // dense-pull entries whose pre cell spiked, since reset
+  unsigned long long plast_updates;  // plastic synapses updated (dw computed), since reset
 };
 
 constexpr uint32_t kErrRasterOverflow = 1u;
@@ -136,7 +138,7 @@ struct StepArgs {
   const void* push_w;
   const PullUnit* pull_units;
   const PlastDev* plast;          // [n_plast]
-  const PullUnit* stdp_units;     // {plastic projection, first ELL cell}
+  const PullUnit* stdp_units;     // {plastic projection, first of kStdpUnit ELL cells}
   float* su;                      // potential, or the refractory count (pack_u)
   float2* sg;                     // conductances of channels 0 and 1
   int* ring;                      // int2 per cell per slot, viewed as int[2]

@@ -581,7 +581,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     const size_t off_units = bytes;
     for (size_t i = 0; i < s.plast.size(); ++i) {
       const ProjDev& P = s.projs[s.plast[i].k];
-      for (uint32_t o = 0; o < P.ell_n; o += kPullUnit) units.push_back({(uint32_t)i, o});
+      for (uint32_t o = 0; o < P.ell_n; o += kStdpUnit) units.push_back({(uint32_t)i, o});
     }
     bytes = align_up(bytes + std::max<size_t>(units.size(), 1) * sizeof(PullUnit), 256);
     std::vector<size_t> off_w0(s.plast.size()), off_t(s.plast.size());
@@ -1159,7 +1159,10 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
   // copies), 8 B per push item written; deliver = per walked push synapse 4 B
   // word + W weight + 8 B atomic, 8 B per push item read; pull = 4 B per
   // stored dense entry plus, per entry whose pre cell spiked, W weight + 8 B
-  // atomic.
+  // atomic; plasticity = per updated plastic synapse 4 B entry + 4 B value
+  // read + 4 B value write + 4 B base weight + W table weight written (a rule
+  // without a0 / a1_j updates only the rows of posts whose post / teacher
+  // spike is set).
   double upd_bytes = (double)a.n_words * 8.0;
   for (const SegDev& d : s.segs) upd_bytes += d.kind == kSegLif ? 32.0 * d.count : 4.0 * d.count;
   double pull_entries = 0;
@@ -1180,10 +1183,9 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
       SGB_CUDA(cudaEventRecord(ev[0], s.stream));
       SGB_CUDA(launch_update(a, s.stream));
       SGB_CUDA(cudaEventRecord(ev[1], s.stream));
-      if (a.n_plast) {
-        SGB_CUDA(launch_stdp(a, s.deliver_blocks, s.stream));
-        s.launches++;
-      }
+      SGB_CUDA(cudaEventRecord(ev[6], s.stream));
+      SGB_CUDA(launch_stdp(a, s.deliver_blocks, s.stream));
+      SGB_CUDA(cudaEventRecord(ev[7], s.stream));
       SGB_CUDA(cudaEventRecord(ev[4], s.stream));
       SGB_CUDA(launch_pull(a, s.pull_blocks, s.stream));
       SGB_CUDA(cudaEventRecord(ev[5], s.stream));
@@ -1195,10 +1197,13 @@ int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t
       const double items = (double)after.active_count[before.step & 1];
       const double walked = (double)(after.delivered - before.delivered);
       const double pulled = (double)(after.pulled - before.pulled);
+      const double plast_upd = (double)(after.plast_updates - before.plast_updates);
       const double step_bytes[K] = {upd_bytes + items * 8.0, walked * (12.0 + W) + items * 8.0,
-                                    pull_entries * 4.0 + pulled * (8.0 + W)};
+                                    pull_entries * 4.0 + pulled * (8.0 + W),
+                                    plast_upd * (16.0 + W)};
       for (int k = 0; k < K; ++k) {
         if (k == 2 && !a.n_pull_units) continue;
+        if (k == 3 && !a.n_plast) continue;
         float ms = 0.f;
         SGB_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
         tot_ms[k] += ms;

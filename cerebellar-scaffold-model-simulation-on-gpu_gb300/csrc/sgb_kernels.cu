@@ -492,11 +492,21 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
     for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
   }
   if (SUM) {
-    const uint32_t R = a.hist_rows + 1u;
-    for (uint32_t d1 = 0; d1 < a.hist_rows; ++d1) {
-      const uint32_t src = (ix.srow + R - d1) % R;  // row of step t - d1
-      for (uint32_t j = threadIdx.x; j < a.n_swords; j += kPullBlock)
-        s_sum[d1 * a.n_swords + j] = __ldg(a.hsum + (size_t)src * a.n_swords + j);
+    // Only the rows of delays 1 .. ring_slots - 1 are looked up (a longer
+    // history kept for plasticity is not); four words per thread per round
+    // with the loads issued before the stores.
+    const uint32_t R = a.hist_rows + 1u, n = (a.ring_slots - 1u) * a.n_swords;
+    for (uint32_t j0 = threadIdx.x; j0 < n; j0 += 4u * kPullBlock) {
+      uint32_t v[4];
+#pragma unroll
+      for (uint32_t k = 0; k < 4u; ++k) {
+        const uint32_t j = j0 + k * kPullBlock;
+        const uint32_t d1 = j / a.n_swords, w = j - d1 * a.n_swords;
+        v[k] = j < n ? __ldg(a.hsum + (size_t)((ix.srow + R - d1) % R) * a.n_swords + w) : 0u;
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < 4u; ++k)
+        if (j0 + k * kPullBlock < n) s_sum[j0 + k * kPullBlock] = v[k];  // row d1 = step t - d1
     }
     if (threadIdx.x == 0) s_sum[a.hist_rows * a.n_swords] = 0u;  // padding's word
     __syncthreads();
@@ -560,6 +570,86 @@ __device__ __forceinline__ uint32_t hist_bit(const uint32_t* hb, uint32_t off) {
   return (__ldg(hb + (off >> 5)) >> (off & 31u)) & 1u;
 }
 
+// A synapse whose dw is 0 keeps its value and weight bit for bit, so with a0
+// = a1_j = 0 (the reference's own coefficients) only synapses of post cells
+// whose post / teacher spike is set change: a row-major unit whose posts all
+// lack it is skipped after one lookup per post.  Units are kStdpUnit cells
+// (four per lane, loads issued together), so the rows of the few posts that
+// do change spread over many warps; the window's spike count is gathered
+// eight rows at a time.
+template <bool BF16>
+__device__ __forceinline__ bool stdp_post_spiked(const StepArgs& a, const PlastDev& L,
+                                                 const ProjDev& P, const uint32_t* hb,
+                                                 uint32_t post) {
+  const uint32_t so = L.rule == SGB_STDP_TEACHER ? __ldg(L.teacher + post) : P.post_base + post;
+  return so != 0xFFFFFFFFu && hist_bit(hb, so);
+}
+
+// Updates the cells of one unit (the whole warp, four cells per lane).
+template <bool BF16>
+__device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
+                                          const uint32_t* hb, uint32_t pad) {
+  constexpr uint32_t B = kStdpUnit / 32;
+  const uint32_t lane = threadIdx.x & 31u;
+  const PlastDev& L = a.plast[un.proj];
+  const ProjDev& P = a.projs[L.proj];
+  const uint32_t end = min(un.o0 + kStdpUnit, P.ell_n);
+  const bool all = L.a0 != 0.f || L.a1_j != 0.f;  // every synapse may change
+  uint32_t e[B], n_upd = 0;
+  bool sp[B];
+#pragma unroll
+  for (uint32_t k = 0; k < B; ++k) {
+    const uint32_t o = un.o0 + lane + 32u * k;
+    e[k] = o < end ? __ldg(P.ell_syn + o) : pad;
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < B; ++k) {
+    const uint32_t o = un.o0 + lane + 32u * k;
+    sp[k] = e[k] < pad &&
+            stdp_post_spiked<BF16>(a, L, P, hb, P.ell_rowmajor ? o / P.ell_K : o % P.post_count);
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < B; ++k) {
+    if (e[k] >= pad || !(all || sp[k])) continue;  // padding, or dw = 0
+    const uint32_t o = un.o0 + lane + 32u * k;
+    ++n_upd;
+    const bool s_pre = hist_bit(hb, e[k] + a.n_pad) != 0u;
+    uint32_t nwin = 0;  // pre spikes at t - d - j, j < window
+    if (sp[k] && L.a2_ji != 0.f) {
+      for (uint32_t j0 = 0; j0 < L.window; j0 += 8u) {
+        uint32_t bit[8];
+#pragma unroll
+        for (uint32_t j = 0; j < 8u; ++j)
+          bit[j] = j0 + j < L.window ? hist_bit(hb, e[k] + (j0 + j + 1u) * a.n_pad) : 0u;
+#pragma unroll
+        for (uint32_t j = 0; j < 8u; ++j) nwin += bit[j];
+      }
+    }
+    // Reference order: A0, A1_J (pre), A1_I (post / teacher), A2_JI window.
+    float dw = __fadd_rn(0.f, L.a0);
+    if (s_pre) dw = __fadd_rn(dw, L.a1_j);
+    if (sp[k]) dw = __fadd_rn(dw, L.a1_i);
+    for (uint32_t j = 0; j < nwin; ++j) dw = __fadd_rn(dw, L.a2_ji);
+    float v = __fadd_rn(L.val[o], dw);
+    v = v < 0.f ? 0.f : (v > L.v_max ? L.v_max : v);
+    L.val[o] = v;
+    const float tw = __fmul_rn(__ldg(L.w0 + o), v);
+    if (BF16)
+      reinterpret_cast<uint16_t*>(L.w_table)[o] = f32_to_bf16_bits(tw);
+    else
+      reinterpret_cast<float*>(L.w_table)[o] = tw;
+  }
+  n_upd = __reduce_add_sync(kFull, n_upd);
+  if (lane == 0 && n_upd) atomicAdd(&a.ctl->plast_updates, (unsigned long long)n_upd);
+}
+
+// A synapse whose dw is 0 keeps its value and weight bit for bit, so with a0
+// = a1_j = 0 (the reference's own coefficients) only synapses of post cells
+// whose post / teacher spike is set change.  Each warp first tests up to 32
+// of its units at once, one per lane (a row-major unit: the one or two posts
+// it covers), then updates only the units that can change.  Units are
+// kStdpUnit cells, so the rows of the few posts that do change spread over
+// many warps; the window's spike count is gathered eight rows at a time.
 template <bool BF16>
 __global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -567,38 +657,32 @@ __global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
   const StepIdx ix = step_of(a);
   const uint32_t* hb = hist_base(a, ix.hrow);
   const uint32_t pad = a.hist_rows * a.n_pad;
-  for (uint32_t u = gw; u < a.n_stdp_units; u += nw) {
-    const PullUnit un = a.stdp_units[u];
-    const PlastDev& L = a.plast[un.proj];
-    const ProjDev& P = a.projs[L.proj];
-    const uint32_t end = min(un.o0 + kPullUnit, P.ell_n);
-    for (uint32_t o = un.o0 + lane; o < end; o += 32u) {
-      const uint32_t e = __ldg(P.ell_syn + o);
-      if (e >= pad) continue;  // padding
-      const uint32_t post = P.ell_rowmajor ? o / P.ell_K : o % P.post_count;
-      const uint32_t so = L.rule == SGB_STDP_TEACHER ? __ldg(L.teacher + post) : P.post_base + post;
-      const bool s_post = so != 0xFFFFFFFFu && hist_bit(hb, so);
-      const bool s_pre = hist_bit(hb, e + a.n_pad) != 0u;
-      // Reference order: A0, A1_J (pre), A1_I (post / teacher), A2_JI window.
-      float dw = __fadd_rn(0.f, L.a0);
-      if (s_pre) dw = __fadd_rn(dw, L.a1_j);
-      if (s_post) dw = __fadd_rn(dw, L.a1_i);
-      if (s_post && L.a2_ji != 0.f)
-        for (uint32_t k = 0; k < L.window; ++k)
-          if (hist_bit(hb, e + (k + 1u) * a.n_pad)) dw = __fadd_rn(dw, L.a2_ji);
-      float v = __fadd_rn(L.val[o], dw);
-      v = v < 0.f ? 0.f : (v > L.v_max ? L.v_max : v);
-      L.val[o] = v;
-      const float tw = __fmul_rn(__ldg(L.w0 + o), v);
-      if (BF16)
-        reinterpret_cast<uint16_t*>(L.w_table)[o] = f32_to_bf16_bits(tw);
-      else
-        reinterpret_cast<float*>(L.w_table)[o] = tw;
+  for (uint32_t base = gw; base < a.n_stdp_units; base += 32u * nw) {
+    const uint32_t u = base + lane * nw;
+    bool active = false;
+    if (u < a.n_stdp_units) {
+      const PullUnit un = a.stdp_units[u];
+      const PlastDev& L = a.plast[un.proj];
+      const ProjDev& P = a.projs[L.proj];
+      if (L.a0 != 0.f || L.a1_j != 0.f || !P.ell_rowmajor) {
+        active = true;
+      } else {
+        const uint32_t end = min(un.o0 + kStdpUnit, P.ell_n);
+        for (uint32_t p = un.o0 / P.ell_K; p <= (end - 1u) / P.ell_K; ++p)
+          active |= stdp_post_spiked<BF16>(a, L, P, hb, p);
+      }
+    }
+    uint32_t act = __ballot_sync(kFull, active);
+    while (act) {
+      const uint32_t j = __ffs(act) - 1;
+      act &= act - 1;
+      stdp_unit<BF16>(a, a.stdp_units[base + j * nw], hb, pad);
     }
   }
 }
 
-// Plastic values back to 1 and the tables to the initial weights.
+// Plastic values back to their start, v_max (the reference starts at 1, its
+// clamp), and the tables to the matching weights.
 template <bool BF16>
 __global__ void __launch_bounds__(kBlock) k_plast_reset(StepArgs a) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -606,10 +690,10 @@ __global__ void __launch_bounds__(kBlock) k_plast_reset(StepArgs a) {
   for (uint32_t u = gw; u < a.n_stdp_units; u += nw) {
     const PullUnit un = a.stdp_units[u];
     const PlastDev& L = a.plast[un.proj];
-    const uint32_t end = min(un.o0 + kPullUnit, a.projs[L.proj].ell_n);
+    const uint32_t end = min(un.o0 + kStdpUnit, a.projs[L.proj].ell_n);
     for (uint32_t o = un.o0 + lane; o < end; o += 32u) {
-      L.val[o] = 1.f;
-      const float tw = __ldg(L.w0 + o);
+      L.val[o] = L.v_max;
+      const float tw = __fmul_rn(__ldg(L.w0 + o), L.v_max);
       if (BF16)
         reinterpret_cast<uint16_t*>(L.w_table)[o] = f32_to_bf16_bits(tw);
       else

@@ -350,7 +350,7 @@ int write_projection_dat(const Network& net, int32_t proj, const char* path) {
 
 // ---------------------------------------------------------------------------
 // Accumulator scales (see header).
-// Plastic values stay in [0, v_max] with v_max <= 1, so a plastic synapse
+// Plastic values start at v_max and stay in [0, v_max], v_max <= 1, so a plastic synapse
 // never delivers more than its initial weight and the accumulator scales
 // need no headroom.
 int add_plasticity(Network& net, int32_t proj, const sgb_plasticity_params* p) {

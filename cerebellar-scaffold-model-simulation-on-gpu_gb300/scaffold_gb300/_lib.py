@@ -23,7 +23,7 @@ STDP_HEBB, STDP_TEACHER = 0, 1
 WEIGHT_FP32, WEIGHT_BF16 = 0, 1
 EXEC_GRAPH, EXEC_PERSISTENT, EXEC_STREAM = 0, 1, 2
 INPUT_POISSON, INPUT_PERIODIC = 0, 1
-KCLASS_COUNT = 3
+KCLASS_COUNT = 4
 KERNEL_NAMES = {0: "k_update+k_deliver", 1: "k_persistent", 2: "k_persistent_resident",
                 3: "k_persistent_fused"}
 

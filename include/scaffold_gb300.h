@@ -105,7 +105,7 @@ typedef struct sgb_input_params {
 /* Synaptic plasticity of one projection: the reference's STDP rules
  * (SynapticPlasticity.cu:40-120, invoke_stdp_plasticity :123-140; compiled
  * in but switched off there, NumOfPlasticity = 0, struct_enum_def.h:50-53).
- * Every synapse carries a value v (1 at start) that scales its weight; each
+ * Every synapse carries a value v (v_max at start) that scales its weight; each
  * step, after the cells update, every synapse of the projection adds
  *   a0 + a1_j [pre spiked at t - d] + a1_i [post (Hebb) / teacher spiked]
  *      + a2_ji [post / teacher spiked] * #{s < window : pre spiked at t - d - s}
@@ -123,8 +123,8 @@ typedef struct sgb_plasticity_params {
   int32_t teacher_proj;  /* Teacher: projection onto the same post population       */
   int32_t window_steps;  /* pairing window of the a2_ji term (reference: 50), 0..64  */
   float a0, a1_i, a1_j, a2_ji;
-  float v_max;           /* upper clamp, 0 < v_max <= 1 (reference Hebb: 1; Teacher has */
-                         /* none, and its only coefficient depresses)                   */
+  float v_max;           /* start value and upper clamp, 0 < v_max <= 1 (reference: 1;  */
+                         /* its Teacher rule has no upper clamp and only depresses)     */
 } sgb_plasticity_params;
 
 typedef struct sgb_population_info {
@@ -358,11 +358,11 @@ int sgb_sim_launch_count(const sgb_sim* sim, int64_t* launches);
 
 /* Instrumented run: advances n_steps with the per-step kernels launched one by
  * one, each bracketed by CUDA events on the handle's stream, and returns per
- * kernel class (0 update, 1 event-driven delivery, 2 dense pull) the mean
- * device time per launch in microseconds, the mean algorithmic bytes per
- * launch, and the number of launches (0 for the pull without dense
- * projections). */
-#define SGB_KCLASS_COUNT 3
+ * kernel class (0 update, 1 event-driven delivery, 2 dense pull, 3
+ * plasticity) the mean device time per launch in microseconds, the mean
+ * algorithmic bytes per launch, and the number of launches (0 for the pull
+ * without dense projections and for plasticity without plastic ones). */
+#define SGB_KCLASS_COUNT 4
 int sgb_sim_profile(sgb_sim* sim, int32_t n_steps, double* mean_us, double* bytes_per_launch,
                     int64_t* launches);
 

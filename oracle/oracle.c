@@ -213,8 +213,8 @@ int orc_create(const orc_net* net, orc_sim** out) {
     const float scale = ldexpf(1.0f, s->scale_bits[p->post * 2 + p->channel]);
     int dmax = 1;
     for (int64_t q = 0; q < p->n; ++q) {
-      ps->v32[q] = 1.0f;
-      ps->v64[q] = 1.0;
+      ps->v32[q] = pp->v_max;  /* values start at the clamp (reference: 1) */
+      ps->v64[q] = (double)pp->v_max;
       ps->w0[q] = p->weight[q] * scale; /* power of two: exact */
       if (p->delay[q] > dmax) dmax = p->delay[q];
     }

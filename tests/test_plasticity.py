@@ -130,3 +130,21 @@ def test_gpu_plasticity_limits_and_reset():
     c2, _ = sim.loop_n_steps(300)
     assert np.array_equal(c1, c2)
     sim.close()
+
+
+@pytest.mark.gpu
+def test_gpu_plasticity_start_value_and_sparse_rule():
+    """Values start at v_max; with a0 = a1_j = 0 (the reference's Teacher
+    coefficients) only rows of posts whose teacher fired change, and the
+    kernel's skipping of the rest is bit-exact."""
+    net = sg.scaffold(1, 0.25, 4)
+    net.add_plasticity(6, sg.STDP_TEACHER, teacher=8, window=20, a2_ji=-0.004, v_max=0.75)
+    sim = sg.Simulation([net], [4])
+    c, _ = sim.loop_n_steps(400)
+    o = oracle_py.Oracle(oracle_py.describe(net), seed=4)
+    ec, _ = o.run(400)
+    assert np.array_equal(c, ec)
+    v, ev = sim.plastic_values(0, 6), o.plastic_values(6)
+    assert np.array_equal(v.view(np.uint32), ev.view(np.uint32))
+    assert v.max() == np.float32(0.75) and v.min() < np.float32(0.75)
+    sim.close()
