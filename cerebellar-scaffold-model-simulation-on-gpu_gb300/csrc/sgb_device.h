@@ -40,7 +40,7 @@ constexpr uint32_t kPushPostBits = 27;
 constexpr uint32_t kPushPostMask = (1u << kPushPostBits) - 1u;
 // Grid-barrier spin limit (iterations of ~64 ns sleeps): ~1 s, then the
 // kernel records kErrBarrierTimeout and returns.
-constexpr uint32_t kBarrierSpinLimit = 1u << 24;
+constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;  // grid-barrier wait limit (1 s)
 
 enum SegKind : uint32_t { kSegLif = 0, kSegInput = 1 };
 
@@ -155,6 +155,7 @@ struct StepArgs {
   uint32_t ring_slots, hist_rows;
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
+  uint32_t bar_extra;             // tests only: barrier arrivals that never come
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
   uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory
   uint32_t any_push;

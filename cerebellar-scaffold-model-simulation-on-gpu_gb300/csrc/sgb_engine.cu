@@ -268,6 +268,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     return set_error(SGB_ERR_ARG, "unknown default propagation mode %d", cfg.default_prop);
   if (cfg.blocks_per_sm < 0 || cfg.blocks_per_sm > 32)
     return set_error(SGB_ERR_ARG, "blocks_per_sm %d not in 0..32", cfg.blocks_per_sm);
+  if (cfg.barrier_test_extra < 0 || cfg.barrier_test_extra > 1024)
+    return set_error(SGB_ERR_ARG, "barrier_test_extra %d not in 0..1024", cfg.barrier_test_extra);
   for (int32_t i = 0; i < n; ++i)
     if (!nets[i]) return set_error(SGB_ERR_ARG, "network %d is NULL", i);
 
@@ -552,6 +554,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.raster_cap = s.raster_cap;
   a.bf16 = s.bf16 ? 1 : 0;
   a.substeps = cfg.substeps;
+  a.bar_extra = (uint32_t)cfg.barrier_test_extra;
   s.deliver_blocks = 2 * s.sm_count;
   // The cell state is read and rewritten every step; where the device lets
   // this context set L2 aside for persisting accesses, the state window

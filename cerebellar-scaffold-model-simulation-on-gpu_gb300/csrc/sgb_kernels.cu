@@ -726,11 +726,20 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
   return v;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // Grid-wide barrier over co-resident blocks (cooperative launch).  Thread 0
 // of each block publishes its block's writes (fence), arrives on a counter,
-// then waits -- at most kBarrierSpinLimit polls -- for all blocks of this
-// round.  On timeout it records kErrBarrierTimeout; every block then returns
-// at its next barrier, so the kernel always ends.
+// then waits for all blocks of this round (plus a.bar_extra arrivals that no
+// block makes, in the tests of this limit) -- at most kBarrierTimeoutNs of
+// global time, checked every 256 polls.  On timeout it records
+// kErrBarrierTimeout; every block then returns at its next barrier (or as
+// soon as it sees the flag), so the kernel always ends and the host reads
+// the flag as SGB_ERR_DEVICE.
 __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long long& target) {
   __shared__ int abort_flag;
   __syncthreads();
@@ -739,12 +748,18 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
     int ok = 1;
     __threadfence();
     atomicAdd(a.bar, 1ull);
+    const unsigned long long want = target + a.bar_extra;
+    unsigned long long t0 = 0;
     uint32_t it = 0;
-    while (ld_acquire(a.bar) < target) {
-      if (++it > kBarrierSpinLimit || (it % 4096 == 0 && (__ldcg(&a.ctl->error) & kErrBarrierTimeout))) {
-        atomicOr(&a.ctl->error, kErrBarrierTimeout);
-        ok = 0;
-        break;
+    while (ld_acquire(a.bar) < want) {
+      if ((++it & 255u) == 0u) {
+        const unsigned long long now = global_ns();
+        if (t0 == 0) t0 = now;
+        if (now - t0 > kBarrierTimeoutNs || (__ldcg(&a.ctl->error) & kErrBarrierTimeout)) {
+          atomicOr(&a.ctl->error, kErrBarrierTimeout);
+          ok = 0;
+          break;
+        }
       }
       __nanosleep(32);
     }

@@ -38,7 +38,8 @@ class Config(C.Structure):
     _fields_ = [("dt_ms", C.c_double), ("substeps", C.c_int32), ("weight_type", C.c_int32),
                 ("exec_mode", C.c_int32), ("chunk_steps", C.c_int32), ("device", C.c_int32),
                 ("default_prop", C.c_int32), ("raster", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("l2_persist", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("l2_persist", C.c_int32), ("barrier_test_extra", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class InputParams(C.Structure):

@@ -239,7 +239,7 @@ class Simulation:
                  dt_ms: float = 0.1, substeps: int = 1, weight_type: int = L.WEIGHT_FP32,
                  exec_mode: int = L.EXEC_GRAPH, chunk_steps: int = 1000, device: int = 0,
                  default_prop: int = L.PROP_AUTO, raster: bool = False, blocks_per_sm: int = 0,
-                 l2_persist: bool = True):
+                 l2_persist: bool = True, barrier_test_extra: int = 0):
         cfg = L.Config()
         L.lib().sgb_config_init(C.byref(cfg))
         cfg.dt_ms = dt_ms
@@ -252,6 +252,7 @@ class Simulation:
         cfg.raster = 1 if raster else 0
         cfg.blocks_per_sm = blocks_per_sm
         cfg.l2_persist = 1 if l2_persist else 0
+        cfg.barrier_test_extra = barrier_test_extra
         self.nets = list(nets)
         n = len(self.nets)
         arr = (C.c_void_p * n)(*[x.handle.value for x in self.nets])

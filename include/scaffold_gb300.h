@@ -90,7 +90,11 @@ typedef struct sgb_config {
   int32_t blocks_per_sm; /* persistent driver: resident blocks per SM (0: 1)              */
   int32_t l2_persist;    /* 1 (default): keep the cell state in a persisting L2 window    */
                          /* (within this process's context); 0: plain caching          */
-  int32_t reserved[7];
+  int32_t barrier_test_extra; /* tests of the bounded wait only: the persistent kernels'   */
+                         /* grid barrier waits for this many arrivals beyond the grid, so */
+                         /* it runs out its 1 s limit and the run returns SGB_ERR_DEVICE; */
+                         /* 0 (default) otherwise                                         */
+  int32_t reserved[6];
 } sgb_config;
 
 typedef struct sgb_input_params {
