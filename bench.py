@@ -184,6 +184,44 @@ def cpu_baseline(wl: dict, sample_steps: int):
                       f"OpenMP over post cells"}
 
 
+def config1_leg(steps: int = 10_000):
+    """Config 1 (9,256 cells, 196,960 synapses, FP32) over its full 1 s of
+    biological time (10,000 exchange steps): the GPU path (one persistent
+    launch per 1,000 steps, CUDA events) and the reference CPU path on all
+    host cores, both over the whole run."""
+    import torch
+
+    import oracle_py
+    import scaffold_gb300 as sg
+
+    net = sg.scaffold(1, 1.0, 1)
+    sim = sg.Simulation([net], [1], exec_mode=sg.EXEC_PERSISTENT, chunk_steps=1000)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.run(1000)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.enqueue(steps)
+    e1.record(stream)
+    sim.sync()
+    torch.cuda.synchronize()
+    gpu_rtf = steps * 1e-4 / (e0.elapsed_time(e1) * 1e-3)
+    sim.close()
+    desc = oracle_py.describe(net)
+    threads = os.cpu_count() or 1
+    if oracle_py.have_ref_harness(1):
+        ref, kind = oracle_py.RefHarness(desc, seed=1), "reference"
+    else:
+        ref, kind = oracle_py.RefPort(desc, seed=1), "port"
+    t0 = time.perf_counter()
+    ref.run(steps, threads=threads)
+    cpu_rtf = steps * 1e-4 / (time.perf_counter() - t0)
+    return {"workload": "config 1: 9,256 cells, 196,960 synapses, FP32, 10,000 steps",
+            "gpu_realtime_factor": gpu_rtf, "cpu_realtime_factor": cpu_rtf, "cpu_kind": kind,
+            "cpu_cores": threads}
+
+
 def stream_copy_gbs(nbytes: int, reps: int = 20) -> float:
     """Bandwidth (read + write bytes) of a plain device copy of a buffer of
     `nbytes`: the measured-peak method at this launch size."""
@@ -452,9 +490,12 @@ def run_gb300(a):
     ell = None if a.no_ell_roofline else ell_roofline(peak)
     plast = None if a.no_ell_roofline else plasticity_leg(peak)
     cpu = None
+    c1 = None
     if not a.no_cpu_baseline:
         try:
             cpu = cpu_baseline(wl, a.cpu_sample)
+            if a.workload == "c2":
+                c1 = config1_leg()
         except Exception as ex:  # report, do not fail the GPU number
             cpu = {"value": None, "error": str(ex)}
     line = {
@@ -484,6 +525,7 @@ def run_gb300(a):
         "phase_profile": phases,
         "dense_ell_roofline": ell,
         "plasticity": plast,
+        "config1": c1,
         "cpu_baseline": cpu,
         "clocks": clk,
     }

@@ -371,6 +371,21 @@ int sgb_sim_get_propagation(const sgb_sim* sim, int32_t net, int32_t proj, int32
   return SGB_OK;
 }
 
+int sgb_sim_checkpoint_size(const sgb_sim* sim, int64_t* bytes) {
+  SIM_CHECK(sim);
+  SGB_GUARD(return sim_checkpoint_size(*sim->sim, bytes);)
+}
+
+int sgb_sim_save_checkpoint(sgb_sim* sim, void* buf, int64_t capacity) {
+  SIM_CHECK(sim);
+  SGB_GUARD(return sim_checkpoint(*sim->sim, buf, capacity, false);)
+}
+
+int sgb_sim_load_checkpoint(sgb_sim* sim, const void* buf, int64_t size) {
+  SIM_CHECK(sim);
+  SGB_GUARD(return sim_checkpoint(*sim->sim, const_cast<void*>(buf), size, true);)
+}
+
 int sgb_sim_plastic_values(sgb_sim* sim, int32_t net, int32_t proj, float* values) {
   SIM_CHECK(sim);
   SGB_GUARD(return sim_plastic_values(*sim->sim, net, proj, values);)

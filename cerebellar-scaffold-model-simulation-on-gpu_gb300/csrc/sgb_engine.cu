@@ -1247,3 +1247,110 @@ int sim_plastic_values(Sim& s, int32_t net, int32_t proj, float* values) {
 }
 
 }  // namespace sgb
+
+namespace sgb {
+
+// ---------------------------------------------------------------------------
+// Checkpoints: a header with a layout signature, then the device regions in
+// a fixed order and the host copy of the stimulus sources.
+namespace {
+struct CkptHeader {
+  char magic[8];          // "SGBCKPT1"
+  uint64_t signature;     // layout hash (cells, delays, history, tables, plasticity)
+  uint64_t bytes;         // whole checkpoint
+};
+
+struct CkptPart {
+  void* dev;
+  size_t n;
+};
+
+uint64_t ckpt_signature(const Sim& s) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](uint64_t v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (v >> (8 * i)) & 0xFFu;
+      h *= 1099511628211ull;
+    }
+  };
+  mix(s.n_pad);
+  mix(s.ring_slots);
+  mix(s.hist_rows);
+  mix(s.segs.size());
+  mix(s.srcs.size());
+  mix(s.projs.size());
+  mix(s.bf16 ? 1 : 0);
+  for (const SegDev& d : s.segs) mix(((uint64_t)d.base << 32) | d.count);
+  for (size_t k = 0; k < s.projs.size(); ++k) mix(((uint64_t)s.projs[k].ell_n << 32) ^ (uint64_t)s.ptab[k].nnz);
+  for (const PlastHost& ph : s.plast) mix(((uint64_t)ph.k << 32) | ph.cells);
+  return h;
+}
+
+std::vector<CkptPart> ckpt_parts(const Sim& s) {
+  const StepArgs& a = s.args;
+  std::vector<CkptPart> v = {{a.su, (size_t)s.n_pad * sizeof(float)},
+                             {a.sg, (size_t)s.n_pad * sizeof(float2)},
+                             {a.ring, (size_t)s.ring_slots * s.n_pad * 8},
+                             {a.hist, s.hist_bytes},
+                             {a.ctl, sizeof(Ctl)},
+                             {a.totals, s.segs.size() * sizeof(double)}};
+  const size_t wsz = s.bf16 ? 2 : 4;
+  for (const PlastHost& ph : s.plast) {
+    v.push_back({(char*)s.d_plast + ph.off_val, ph.cells * 4});
+    v.push_back({const_cast<void*>(s.projs[ph.k].ell_w), ph.cells * wsz});
+  }
+  return v;
+}
+}  // namespace
+
+int sim_checkpoint_size(const Sim& s, int64_t* bytes) {
+  if (!bytes) return set_error(SGB_ERR_ARG, "bytes is NULL");
+  size_t n = sizeof(CkptHeader) + s.srcs.size() * sizeof(SrcDev);
+  for (const CkptPart& p : ckpt_parts(s)) n += p.n;
+  *bytes = (int64_t)n;
+  return SGB_OK;
+}
+
+int sim_checkpoint(Sim& s, void* buf, int64_t size, bool load) {
+  if (!buf) return set_error(SGB_ERR_ARG, "buffer is NULL");
+  int64_t need = 0;
+  sim_checkpoint_size(s, &need);
+  if (size < need)
+    return set_error(SGB_ERR_ARG, "checkpoint buffer of %lld bytes, %lld needed", (long long)size,
+                     (long long)need);
+  char* p = (char*)buf;
+  CkptHeader h;
+  if (load) {
+    memcpy(&h, p, sizeof h);
+    if (memcmp(h.magic, "SGBCKPT1", 8) != 0) return set_error(SGB_ERR_FORMAT, "not a checkpoint");
+    if (h.signature != ckpt_signature(s) || h.bytes != (uint64_t)need)
+      return set_error(SGB_ERR_FORMAT, "checkpoint of a different network layout");
+  } else {
+    memcpy(h.magic, "SGBCKPT1", 8);
+    h.signature = ckpt_signature(s);
+    h.bytes = (uint64_t)need;
+    memcpy(p, &h, sizeof h);
+  }
+  p += sizeof h;
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  for (const CkptPart& part : ckpt_parts(s)) {
+    if (load)
+      SGB_CUDA(cudaMemcpy(part.dev, p, part.n, cudaMemcpyHostToDevice));
+    else
+      SGB_CUDA(cudaMemcpy(p, part.dev, part.n, cudaMemcpyDeviceToHost));
+    p += part.n;
+  }
+  const size_t nsrc = s.srcs.size() * sizeof(SrcDev);
+  if (load) {
+    if (nsrc) {
+      memcpy(s.srcs.data(), p, nsrc);
+      memcpy(s.h_srcs, s.srcs.data(), nsrc);
+      SGB_CUDA(cudaMemcpy((void*)s.args.srcs, s.h_srcs, nsrc, cudaMemcpyHostToDevice));
+    }
+  } else if (nsrc) {
+    memcpy(p, s.srcs.data(), nsrc);
+  }
+  return SGB_OK;
+}
+
+}  // namespace sgb

@@ -99,6 +99,8 @@ int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode);
 int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path);
 int sim_profile(Sim& s, int32_t n_steps, double* mean_us, double* bytes, int64_t* launches);
 int sim_plastic_values(Sim& s, int32_t net, int32_t proj, float* values);
+int sim_checkpoint_size(const Sim& s, int64_t* bytes);
+int sim_checkpoint(Sim& s, void* buf, int64_t size, bool load);
 int sim_set_stream(Sim& s, cudaStream_t st);
 
 }  // namespace sgb

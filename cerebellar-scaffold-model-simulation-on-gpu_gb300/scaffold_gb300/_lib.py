@@ -123,6 +123,9 @@ PROTOTYPES = {
     "sgb_net_add_plasticity": (C.c_int, [vp, i32, P(PlasticityParams)]),
     "sgb_net_plasticity_info": (C.c_int, [vp, i32, i32p, P(PlasticityParams)]),
     "sgb_sim_plastic_values": (C.c_int, [vp, i32, i32, f32p]),
+    "sgb_sim_checkpoint_size": (C.c_int, [vp, i64p]),
+    "sgb_sim_save_checkpoint": (C.c_int, [vp, vp, i64]),
+    "sgb_sim_load_checkpoint": (C.c_int, [vp, vp, i64]),
     "sgb_sim_create": (C.c_int, [P(Config), P(vp), P(C.c_uint64), i32, P(vp)]),
     "sgb_sim_destroy": (None, [vp]),
     "sgb_sim_set_stream": (C.c_int, [vp, vp]),

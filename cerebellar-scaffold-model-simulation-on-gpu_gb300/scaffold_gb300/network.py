@@ -381,6 +381,19 @@ class Simulation:
         L.check(L.lib().sgb_sim_spike_totals(self._h, _ptr(t, C.c_double)))
         return t
 
+    def save_checkpoint(self) -> bytes:
+        """The handle's whole evolving state as bytes (at a chunk boundary)."""
+        n = C.c_int64()
+        L.check(L.lib().sgb_sim_checkpoint_size(self._h, C.byref(n)))
+        buf = (C.c_char * n.value)()
+        L.check(L.lib().sgb_sim_save_checkpoint(self._h, buf, n.value))
+        return bytes(buf)
+
+    def load_checkpoint(self, data: bytes) -> None:
+        """Restores a checkpoint of a handle with the same networks and configuration."""
+        buf = (C.c_char * len(data)).from_buffer_copy(data)
+        L.check(L.lib().sgb_sim_load_checkpoint(self._h, buf, len(data)))
+
     def plastic_values(self, net: int, proj: int) -> np.ndarray:
         """Plasticity values of a plastic projection's synapses (synapse order)."""
         n = self.nets[net].synapses(proj)[0].size

@@ -330,6 +330,20 @@ int sgb_sim_segment_info(const sgb_sim* sim, int32_t seg, sgb_segment_info* info
 int sgb_sim_get_state(sgb_sim* sim, float* u, float* g, int32_t* ref);
 int sgb_sim_set_state(sgb_sim* sim, const float* u, const float* g, const int32_t* ref);
 
+/* Checkpoint / resume.  A checkpoint holds the whole evolving device state of
+ * a handle: cell state, pending synaptic increments, spike history, step and
+ * event counters, long-horizon totals, stimulus rates and plastic values.
+ * sgb_sim_checkpoint_size gives its size; save copies it into caller memory
+ * (at a chunk boundary: after sgb_sim_run or sgb_sim_sync); load restores it
+ * into a handle built from the same networks and configuration, which then
+ * continues exactly as the saved one would have when its seeds are the same
+ * (inputs are keyed on seed, cell and step).  The reference has no
+ * counterpart (ResetNetworkEnv, GPUScaffoldSimulation.cu:802-854, only
+ * re-draws the potentials). */
+int sgb_sim_checkpoint_size(const sgb_sim* sim, int64_t* bytes);
+int sgb_sim_save_checkpoint(sgb_sim* sim, void* buf, int64_t capacity);
+int sgb_sim_load_checkpoint(sgb_sim* sim, const void* buf, int64_t size);
+
 /* Writes a raster returned by sgb_sim_run in the reference's text format,
  * one "t\tlocal_id\ttype_id" line per spike (print_spike_train,
  * GPUScaffoldSimulation.cu:77-85): t in ms as %f (step index first_step + k
