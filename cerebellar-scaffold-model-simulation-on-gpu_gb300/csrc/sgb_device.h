@@ -114,7 +114,7 @@ struct PlastDev {
   uint32_t proj;                  // index into projs
   uint32_t rule;                  // SGB_STDP_HEBB / SGB_STDP_TEACHER
   uint32_t window;                // pairing window (steps)
-  uint32_t pad_;
+  uint32_t recent_ok;             // max delay + window <= 64: use the spike registers
   float a0, a1_i, a1_j, a2_ji, v_max, pad2_;
   float* val;
   const float* w0;
@@ -143,6 +143,7 @@ struct StepArgs {
   float2* sg;                     // conductances of channels 0 and 1
   int* ring;                      // int2 per cell per slot, viewed as int[2]
   uint32_t* hist;                 // [2H][n_words]: rows H-1-(t mod H) and 2H-1-(t mod H) hold step t
+  unsigned long long* recent;     // [n_pad] last 64 steps of spikes per cell (plasticity), or NULL
   uint32_t* hsum;                 // [H + 1][n_swords]: bit w of row t mod (H + 1) = word w
                                   // of step t had a spike
   uint2* items;                   // [2][item_cap] push work ranges

@@ -340,7 +340,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   s.ring_slots = (uint32_t)max_delay + 1;
   s.hist_rows = (uint32_t)max_delay;
   // A plastic synapse with delay d reads its pre cell's spikes d .. d +
-  // window - 1 steps back, a teacher up to max_delay steps back.
+  // window - 1 steps back, a teacher up to max_delay steps back.  Windows that
+  // end within 64 steps come from the per-cell spike registers instead.
   bool any_plastic = false;
   for (const Network& net : s.nets)
     for (const Projection& pr : net.projs) {
@@ -348,8 +349,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       any_plastic = true;
       int dmax = 1;
       for (uint8_t d : pr.delay) dmax = std::max(dmax, (int)d);
-      s.hist_rows = std::max<uint32_t>(
-          s.hist_rows, (uint32_t)std::max(max_delay + 1, dmax + pr.plast.window_steps));
+      const int back = dmax + pr.plast.window_steps <= 64 ? 0 : dmax + pr.plast.window_steps;
+      s.hist_rows = std::max<uint32_t>(s.hist_rows, (uint32_t)std::max(max_delay + 1, back));
     }
   if (any_plastic && cfg.exec_mode == SGB_EXEC_PERSISTENT)
     return set_error(SGB_ERR_UNSUPPORTED,
@@ -587,6 +588,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       for (uint32_t o = 0; o < P.ell_n; o += kStdpUnit) units.push_back({(uint32_t)i, o});
     }
     bytes = align_up(bytes + std::max<size_t>(units.size(), 1) * sizeof(PullUnit), 256);
+    s.off_recent = bytes;
+    bytes = align_up(bytes + (size_t)s.n_pad * 8, 256);
     std::vector<size_t> off_w0(s.plast.size()), off_t(s.plast.size());
     for (size_t i = 0; i < s.plast.size(); ++i) {
       PlastHost& ph = s.plast[i];
@@ -629,6 +632,11 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
       d.proj = ph.k;
       d.rule = (uint32_t)q.rule;
       d.window = (uint32_t)q.window_steps;
+      {
+        int dmax = 1;
+        for (uint8_t dl : pr.delay) dmax = std::max(dmax, (int)dl);
+        d.recent_ok = dmax + q.window_steps <= 64 ? 1u : 0u;
+      }
       d.a0 = q.a0;
       d.a1_i = q.a1_i;
       d.a1_j = q.a1_j;
@@ -644,6 +652,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     if (!units.empty())
       SGB_CUDA(cudaMemcpy(pb + off_units, units.data(), units.size() * sizeof(PullUnit), cudaMemcpyHostToDevice));
     a.plast = (const PlastDev*)pb;
+    a.recent = (unsigned long long*)(pb + s.off_recent);
     a.n_plast = (uint32_t)pd.size();
     a.stdp_units = (const PullUnit*)(pb + off_units);
     a.n_stdp_units = (uint32_t)units.size();
@@ -699,7 +708,10 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
   SGB_CUDA(cudaMemsetAsync(a.ring, 0, (size_t)s.ring_slots * s.n_pad * 8, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.hist, 0, s.hist_bytes, s.stream));
   SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
-  if (a.n_plast) SGB_CUDA(launch_plast_reset(a, s.deliver_blocks, s.stream));
+  if (a.n_plast) {
+    SGB_CUDA(launch_plast_reset(a, s.deliver_blocks, s.stream));
+    SGB_CUDA(cudaMemsetAsync(a.recent, 0, (size_t)s.n_pad * 8, s.stream));
+  }
   SGB_CUDA(cudaMemsetAsync(a.items, 0, (size_t)2 * a.item_cap * sizeof(uint2), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.totals, 0, s.segs.size() * sizeof(double), s.stream));
   SGB_CUDA(cudaStreamSynchronize(s.stream));
@@ -1295,6 +1307,7 @@ std::vector<CkptPart> ckpt_parts(const Sim& s) {
                              {a.ctl, sizeof(Ctl)},
                              {a.totals, s.segs.size() * sizeof(double)}};
   const size_t wsz = s.bf16 ? 2 : 4;
+  if (!s.plast.empty()) v.push_back({a.recent, (size_t)s.n_pad * 8});
   for (const PlastHost& ph : s.plast) {
     v.push_back({(char*)s.d_plast + ph.off_val, ph.cells * 4});
     v.push_back({const_cast<void*>(s.projs[ph.k].ell_w), ph.cells * wsz});

@@ -66,6 +66,7 @@ struct Sim {
   int persistent_blocks = 0;
   // Plasticity (STDP) of plastic projections.
   void* d_plast = nullptr;
+  size_t off_recent = 0;      // per-cell spike registers inside d_plast
   std::vector<PlastHost> plast;
   // Persisting L2 window over the cell state (su, sg).
   void* l2_base = nullptr;

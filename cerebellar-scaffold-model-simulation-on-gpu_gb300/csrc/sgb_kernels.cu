@@ -266,6 +266,9 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
       fired = lif_update(sd, a.substeps, st, in.acc);
       state_out(a, i, st);
     }
+    // Handles with plastic projections (per-step drivers only): each cell's
+    // last 64 steps of spikes, bit j = step t - j, for the pairing windows.
+    if (a.recent) a.recent[i] = (a.recent[i] << 1) | (fired ? 1ull : 0ull);
   }
   uint32_t r0 = 0, r1 = 0, od = 0;
   if (fired) {
@@ -613,16 +616,27 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
     if (e[k] >= pad || !(all || sp[k])) continue;  // padding, or dw = 0
     const uint32_t o = un.o0 + lane + 32u * k;
     ++n_upd;
-    const bool s_pre = hist_bit(hb, e[k] + a.n_pad) != 0u;
+    bool s_pre;
     uint32_t nwin = 0;  // pre spikes at t - d - j, j < window
-    if (sp[k] && L.a2_ji != 0.f) {
-      for (uint32_t j0 = 0; j0 < L.window; j0 += 8u) {
-        uint32_t bit[8];
+    if (L.recent_ok) {
+      // The pre cell's spike register: bit d is step t - d, bits d .. d +
+      // window - 1 the window (d + window <= 64 for this projection).
+      const uint32_t d = e[k] / a.n_pad + 1u, g = e[k] - (d - 1u) * a.n_pad;
+      const unsigned long long r = a.recent[g] >> d;
+      s_pre = (r & 1ull) != 0ull;
+      if (sp[k] && L.a2_ji != 0.f)
+        nwin = __popcll(L.window == 64u ? r : r & ((1ull << L.window) - 1ull));
+    } else {
+      s_pre = hist_bit(hb, e[k] + a.n_pad) != 0u;
+      if (sp[k] && L.a2_ji != 0.f) {
+        for (uint32_t j0 = 0; j0 < L.window; j0 += 8u) {
+          uint32_t bit[8];
 #pragma unroll
-        for (uint32_t j = 0; j < 8u; ++j)
-          bit[j] = j0 + j < L.window ? hist_bit(hb, e[k] + (j0 + j + 1u) * a.n_pad) : 0u;
+          for (uint32_t j = 0; j < 8u; ++j)
+            bit[j] = j0 + j < L.window ? hist_bit(hb, e[k] + (j0 + j + 1u) * a.n_pad) : 0u;
 #pragma unroll
-        for (uint32_t j = 0; j < 8u; ++j) nwin += bit[j];
+          for (uint32_t j = 0; j < 8u; ++j) nwin += bit[j];
+        }
       }
     }
     // Reference order: A0, A1_J (pre), A1_I (post / teacher), A2_JI window.

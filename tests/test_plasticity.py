@@ -133,6 +133,25 @@ def test_gpu_plasticity_limits_and_reset():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("window", [40, 64])
+def test_gpu_plasticity_window_sources(window):
+    """Windows ending within 64 steps are counted from the per-cell spike
+    registers, longer ones (window 64 with any delay) from the spike history;
+    both agree with the oracle bit for bit."""
+    net = sg.scaffold(1, 0.25, 7)
+    net.add_plasticity(2, sg.STDP_HEBB, window=window, a1_i=0.001, a2_ji=-0.003)
+    sim = sg.Simulation([net], [7], chunk_steps=150)
+    c, _ = sim.loop_n_steps(450)
+    o = oracle_py.Oracle(oracle_py.describe(net), seed=7)
+    ec, _ = o.run(450)
+    assert np.array_equal(c, ec)
+    v, ev = sim.plastic_values(0, 2), o.plastic_values(2)
+    assert np.array_equal(v.view(np.uint32), ev.view(np.uint32))
+    assert (v != 1).any()
+    sim.close()
+
+
+@pytest.mark.gpu
 def test_gpu_plasticity_start_value_and_sparse_rule():
     """Values start at v_max; with a0 = a1_j = 0 (the reference's Teacher
     coefficients) only rows of posts whose teacher fired change, and the
