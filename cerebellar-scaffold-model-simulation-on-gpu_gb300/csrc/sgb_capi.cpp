@@ -317,6 +317,7 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
   info->step_kernel = s.cfg.exec_mode == SGB_EXEC_PERSISTENT
                           ? persistent_kernel_kind(s.args, s.persistent_blocks)
                           : SGB_KERNEL_GRAPH;
+  info->push_smem_bytes = info->step_kernel == SGB_KERNEL_FUSED ? (int32_t)s.args.row_smem : 0;
   info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;
   info->weight_type = s.cfg.weight_type;

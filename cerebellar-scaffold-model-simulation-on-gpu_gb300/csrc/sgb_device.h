@@ -162,6 +162,7 @@ struct StepArgs {
   uint32_t any_push;
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer
+  uint32_t row_smem;              // fused persistent kernel: shared-memory bytes for push rows (0: none)
   int32_t bf16;
   int32_t substeps;
 };
@@ -174,6 +175,10 @@ cudaError_t launch_deliver(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s);
 // One cooperative launch advancing n_steps; grid = blocks (all co-resident).
 cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, cudaStream_t s);
+// Largest dynamic shared memory the fused persistent kernel can take for push
+// rows, and setting it (both weight types) before launches that use it.
+uint32_t fused_row_smem_max();
+cudaError_t set_fused_row_smem(uint32_t bytes);
 int persistent_blocks_per_sm(bool bf16);
 // Dense pull (per-step driver): k_pull needs pull_setup() once per device
 // before its first launch.

@@ -244,6 +244,23 @@ static int upload_modes(Sim& s) {
     SGB_CUDA(cudaMemcpy((void*)a.pull_units, units.data(), units.size() * sizeof(PullUnit), cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
   a.n_pull_units = (uint32_t)units.size();
+  // Fused persistent kernel: shared memory for the push rows of the block
+  // holding the most synapses (word slot ws runs in block ws mod blocks).
+  a.row_smem = 0;
+  if (total > 0 && s.persistent_blocks > 0 &&
+      persistent_kernel_kind(a, s.persistent_blocks) == SGB_KERNEL_FUSED) {
+    std::vector<uint64_t> need((size_t)s.persistent_blocks, 0);
+    for (size_t ws = 0; ws < s.upd_words.size(); ++ws) {
+      const uint32_t w = s.upd_words[ws];
+      need[ws % need.size()] += row[(size_t)w * 32 + 32] - row[(size_t)w * 32];
+    }
+    const uint64_t most = *std::max_element(need.begin(), need.end()) * sizeof(uint2);
+    const uint64_t bytes = std::min<uint64_t>((most + 255) & ~255ull, fused_row_smem_max());
+    if (bytes >= 1024) {
+      SGB_CUDA(set_fused_row_smem((uint32_t)bytes));
+      a.row_smem = (uint32_t)bytes;
+    }
+  }
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
   return SGB_OK;
@@ -674,6 +691,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   SGB_CUDA(cudaMemcpy((void*)a.outdeg, outdeg.data(), outdeg.size() * 4, cudaMemcpyHostToDevice));
   if (!upd_words.empty())
     SGB_CUDA(cudaMemcpy((void*)a.upd_words, upd_words.data(), upd_words.size() * 4, cudaMemcpyHostToDevice));
+  s.upd_words = upd_words;
   int rc = upload_modes(s);
   if (rc) return rc;
 

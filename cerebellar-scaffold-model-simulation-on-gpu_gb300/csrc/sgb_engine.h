@@ -64,6 +64,7 @@ struct Sim {
   int pull_blocks = 0;        // k_pull grid (resident blocks per SM x SMs)
   size_t hist_bytes = 0;      // spike history + its summary
   int persistent_blocks = 0;
+  std::vector<uint32_t> upd_words;  // host copy of args.upd_words
   // Plasticity (STDP) of plastic projections.
   void* d_plast = nullptr;
   size_t off_recent = 0;      // per-cell spike registers inside d_plast

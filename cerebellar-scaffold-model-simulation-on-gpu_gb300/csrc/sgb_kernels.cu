@@ -331,6 +331,27 @@ __device__ __forceinline__ uint32_t push_item(const StepArgs& a, uint2 it, uint3
   return it.y >> 23;
 }
 
+// The same from a block's shared-memory copy of its cells' rows: {synapse
+// word, fixed-point increment} per synapse, so the item's only memory round
+// trip is its atomics.
+__device__ __forceinline__ uint32_t push_item_smem(const StepArgs& a, const uint2* rows, uint2 it,
+                                                   uint32_t slot0) {
+  constexpr int kPer = kPushChunk / 32;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t n = it.y >> 23;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    const uint32_t j = k * 32 + lane;
+    if (j >= n) break;
+    const uint2 e = rows[it.x + j];
+    uint32_t slot = slot0 + ((e.x >> kPushPostBits) & 15u);
+    if (slot >= a.ring_slots) slot -= a.ring_slots;
+    atomicAdd(a.ring + (((size_t)slot * a.n_pad + (e.x & kPushPostMask)) << 1) + (e.x >> 31),
+              (int)e.y);
+  }
+  return n;
+}
+
 // ---- dense pull (ELL) ----------------------------------------------------------
 // A unit is kPullUnit consecutive entries of one projection's ELL, whatever
 // its layout.  An entry is the offset of its spike bit above the step's
@@ -894,7 +915,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
 // reads slot t, so update and push of the same step share one phase and a
 // step needs one grid barrier.  Each block gathers the push items of its
 // spiking cells in shared memory, so the rows of a cell with thousands of
-// synapses spread over the block's 32 warps.
+// synapses spread over the block's 32 warps.  With a.row_smem > 0 the block
+// first copies its cells' push rows into dynamic shared memory (in word, lane
+// order, each row whole or not at all; rows past the capacity stay in global
+// memory), so a step's pushes read no global memory.
 constexpr uint32_t kBlockItems = 2048;  // push items per block and step (16 KiB)
 
 template <bool BF16>
@@ -902,6 +926,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
                                                                        uint32_t n_steps) {
   __shared__ uint2 s_items[kBlockItems];
   __shared__ uint32_t s_n[2];  // item count of step parity p; the other one is reset
+  __shared__ uint32_t s_wsum[kPersistBlock / 32];
+  extern __shared__ uint2 s_rows[];
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -928,6 +954,43 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       od = __ldg(a.outdeg + i);
       r0 = __ldg(a.push_row + i);
       r1 = __ldg(a.push_row + i + 1);
+    }
+  }
+  // Push rows into shared memory: sb = the row's offset there, or kNoRow.
+  constexpr uint32_t kNoRow = 0xFFFFFFFFu;
+  uint32_t sb = kNoRow;
+  if (a.row_smem) {
+    const uint32_t len = r1 - r0;
+    uint32_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(kFull, incl, o);
+      if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31) s_wsum[wib] = incl;
+    __syncthreads();
+    if (wib == 0) {
+      uint32_t x = s_wsum[lane], xi = x;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, xi, o);
+        if (lane >= (uint32_t)o) xi += v;
+      }
+      s_wsum[lane] = xi - x;
+    }
+    __syncthreads();
+    const uint32_t base = s_wsum[wib] + incl - len;
+    const uint32_t cap = a.row_smem / (uint32_t)sizeof(uint2);
+    if (len && base <= cap && len <= cap - base) sb = base;
+    uint32_t todo = __ballot_sync(kFull, sb != kNoRow);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      todo &= todo - 1;
+      const uint32_t q0 = __shfl_sync(kFull, r0, src), n = __shfl_sync(kFull, len, src);
+      const uint32_t b0 = __shfl_sync(kFull, sb, src);
+      for (uint32_t k = lane; k < n; k += 32)
+        s_rows[b0 + k] = make_uint2(__ldg(a.push_syn + q0 + k),
+                                    (uint32_t)__float2int_rn(load_weight<BF16>(a.push_w, q0 + k)));
     }
   }
   unsigned long long target = 0;
@@ -965,9 +1028,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
           if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
         }
         off = __shfl_sync(kFull, off, 0) + incl - nit;
+        // Item: (first synapse, length << 23 | 1 when the row is in shared memory).
         for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
-          const uint32_t q0 = r0 + k * kPushChunk;
-          s_items[off + k] = make_uint2(q0, min(kPushChunk, r1 - q0) << 23);
+          const uint32_t q = k * kPushChunk, len = min(kPushChunk, r1 - r0 - q) << 23;
+          s_items[off + k] = sb != kNoRow ? make_uint2(sb + q, len | 1u) : make_uint2(r0 + q, len);
         }
         if (a.raster_cap) {
           roff = __shfl_sync(kFull, roff, 0);
@@ -984,8 +1048,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     const uint32_t n_items = min(s_n[par], kBlockItems);
     // The other parity's count was last read before this step's __syncthreads.
     if (threadIdx.x == 0) s_n[par ^ 1u] = 0;
-    for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32)
-      walked += push_item<BF16>(a, s_items[u], ix.slot);
+    for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32) {
+      const uint2 it = s_items[u];
+      walked += (it.y & 1u) ? push_item_smem(a, s_rows, it, ix.slot)
+                            : push_item<BF16>(a, it, ix.slot);
+    }
     // Items beyond the block's capacity are delivered by the warp that made them.
     uint32_t spill = __ballot_sync(kFull, off + nit > kBlockItems);
     while (spill) {
@@ -1127,7 +1194,28 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                                         : (const void*)k_persistent_resident<false>)
                               : (a.bf16 ? (const void*)k_persistent<true>
                                         : (const void*)k_persistent<false>);
-  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, 0, s);
+  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params,
+                                     fused ? a.row_smem : 0, s);
+}
+
+uint32_t fused_row_smem_max() {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  cudaFuncGetAttributes(&fa, k_persistent_fused<false>);
+  cudaFuncAttributes fb{};
+  cudaFuncGetAttributes(&fb, k_persistent_fused<true>);
+  const size_t st = fa.sharedSizeBytes > fb.sharedSizeBytes ? fa.sharedSizeBytes : fb.sharedSizeBytes;
+  return (size_t)optin > st ? (uint32_t)(((size_t)optin - st) & ~(size_t)255) : 0u;
+}
+
+cudaError_t set_fused_row_smem(uint32_t bytes) {
+  cudaError_t e = cudaFuncSetAttribute(k_persistent_fused<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e) return e;
+  return cudaFuncSetAttribute(k_persistent_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes);
 }
 
 }  // namespace sgb

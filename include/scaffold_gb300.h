@@ -165,7 +165,7 @@ typedef struct sgb_sim_info {
   int64_t events;        /* synaptic events (spikes x out-degree) since the last reset */
   int64_t delivered;     /* synapses walked by event-driven delivery since the last reset */
   int32_t step_kernel;   /* SGB_KERNEL_*: the kernel a chunk of steps runs in            */
-  int32_t reserved_;
+  int32_t push_smem_bytes; /* SGB_KERNEL_FUSED: shared memory per block holding push rows (0: none) */
   int64_t pulled;        /* dense-pull entries whose pre cell had spiked (deliveries) since the last reset */
   int64_t pull_entries;  /* dense-table entries streamed per step (0 without dense projections) */
   int64_t l2_persist_bytes; /* L2 set aside for the persisting state window (0: none)   */

@@ -223,3 +223,35 @@ def test_autotune_keeps_state_and_caches(tmp_path):
     other.autotune(200, cache)  # served from the cache: no new line
     assert [other.get_propagation(0, j) for j in range(len(net.projections))] == modes
     assert len(open(cache).read().splitlines()) == 1
+
+
+@pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
+def test_fused_kernel_rows_partly_in_shared_memory(weight):
+    """The fused persistent kernel copies each block's push rows into shared
+    memory while they fit: 4,864 Poisson cells (one 32-cell word per block)
+    with 1,000 synapses each need 32,000 row entries per block, more than the
+    capacity, so the first rows of a word are read from shared memory and the
+    rest from global memory.  Bit-exact against the oracle either way."""
+    rng = np.random.default_rng(17)
+    net = sg.Network()
+    ch = [(1.0, 0.0, 1.0, 0.5), (1.0, -80.0, 1.0, 10.0)]
+    src = net.set_neuron_params("src", 4864, 0, 0, 0, 0, 0, 0, 0, sg.INPUT)
+    dst = net.set_neuron_params("dst", 2048, 3.0, -70.0, 2.0, 0.0, -70.0, -50.0, 0.2, sg.NORMAL, ch)
+    fan = 1000
+    pre = np.repeat(np.arange(4864, dtype=np.uint32), fan)
+    post = rng.integers(0, 2048, pre.size, dtype=np.uint32)
+    w = rng.uniform(0.02, 0.2, pre.size).astype(np.float32)
+    d = rng.integers(1, 5, pre.size).astype(np.uint8)
+    net.add_projection(src, dst, pre, post, w, d, sg.CH_EXC, sg.PROP_CSR)
+    net.set_input_stim(src, rate_hz=30.0)
+    steps = 300
+    sim = sg.Simulation([net], [5], weight_type=weight, exec_mode=sg.EXEC_PERSISTENT,
+                        raster=True, chunk_steps=150)
+    info = sim.info()
+    assert info.step_kernel == 3  # SGB_KERNEL_FUSED
+    assert 0 < info.push_smem_bytes < 32000 * 8
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
+    exp = _oracle(net, 5, steps, bf16=weight == sg.WEIGHT_BF16)
+    _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    assert counts[:, 1].sum() > 0
+    sim.close()
