@@ -778,14 +778,19 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // most kBarrierTimeoutNs of global time, checked every 256 polls.  On timeout it records
 // kErrBarrierTimeout; every block then returns at its next barrier (or as
 // soon as it sees the flag), so the kernel always ends and the host reads
-// the flag as SGB_ERR_DEVICE.
-__device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long long& target) {
-  __shared__ int abort_flag;
+// the flag as SGB_ERR_DEVICE.  grid_arrive / grid_wait are the two halves,
+// for callers with work that does not depend on the other blocks in between.
+__device__ __forceinline__ void grid_arrive(const StepArgs& a, unsigned long long& target) {
   __syncthreads();
   target += gridDim.x;
+  if (threadIdx.x == 0)
+    asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
+}
+
+__device__ __forceinline__ bool grid_wait(const StepArgs& a, unsigned long long target) {
+  __shared__ int abort_flag;
   if (threadIdx.x == 0) {
     int ok = 1;
-    asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
     const unsigned long long want = target + a.bar_extra;
     unsigned long long t0 = 0;
     uint32_t it = 0;
@@ -805,6 +810,11 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
   }
   __syncthreads();
   return !abort_flag;
+}
+
+__device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long long& target) {
+  grid_arrive(a, target);
+  return grid_wait(a, target);
 }
 
 template <bool BF16>
@@ -938,7 +948,9 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   // block), so every SM holds about the same number of cells and spikes.
   const uint32_t ws = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
   const bool has = ws < a.n_upd_words;
-  uint32_t w = 0, seg = 0, i = 0, local = 0, mask = 0, r0 = 0, r1 = 0, od = 0;
+  // st: a LIF cell's state {u, g0, g1, ref}; an input cell's source mask and
+  // index within its segment (bits of st.x, st.y).
+  uint32_t w = 0, seg = 0, i = 0, r0 = 0, r1 = 0, od = 0;
   bool valid = false, lif = false;
   float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
   if (has) {
@@ -946,16 +958,24 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     seg = __ldg(a.seg_of_word + w);
     i = (w << 5) + lane;
     const SegDev& sd = a.segs[seg];
-    local = i - sd.base;
+    const uint32_t local = i - sd.base;
     valid = local < sd.count;
     lif = sd.kind == kSegLif;
     if (valid) {
-      if (lif) st = state_in(a.su[i], a.sg[i], sd.Vr); else mask = __ldg(a.src_mask + i);
+      if (lif)
+        st = state_in(a.su[i], a.sg[i], sd.Vr);
+      else
+        st = make_float4(__uint_as_float(__ldg(a.src_mask + i)), __uint_as_float(local), 0.f, 0.f);
       od = __ldg(a.outdeg + i);
       r0 = __ldg(a.push_row + i);
       r1 = __ldg(a.push_row + i + 1);
     }
   }
+  // Input cells: the stimulus decision of the coming step, drawn ahead (it
+  // depends only on the step index) -- for later steps while the previous
+  // grid barrier completes.
+  const bool stim = valid && !lif && __float_as_uint(st.x) != 0u;
+  bool next_in = stim && input_fire(a, a.segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), t0);
   // Push rows into shared memory: sb = the row's offset there, or kNoRow.
   constexpr uint32_t kNoRow = 0xFFFFFFFFu;
   uint32_t sb = kNoRow;
@@ -1001,11 +1021,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     ix.t = t0 + s;
     ix.rel = s;
     const uint32_t par = s & 1u;
-    if (a.raster_cap && leader && s > 0) a.raster_off[s] = __ldcg(&ctl->raster_count);
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     uint32_t off = 0, nit = 0;
     if (has) {
-      const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
+      const bool fired = lif ? cell_fire(a, a.segs[seg], i, 0u, valid, st, 0u, ix) : next_in;
       const uint32_t ballot = __ballot_sync(kFull, fired);
       if (lane == 0) put_hist(a, ix, w, ballot);
       if (ballot) {
@@ -1065,16 +1084,55 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         walked += push_item<BF16>(a, make_uint2(q0, min(kPushChunk, b1 - q0) << 23), ix.slot);
       }
     }
-    if (!grid_barrier(a, target)) break;
+    grid_arrive(a, target);
+    if (stim && s + 1 < n_steps)
+      next_in = input_fire(a, a.segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1);
+    if (!grid_wait(a, target)) break;
     ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
     ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
   if (valid && lif) state_out(a, i, st);
+  // Raster offsets: with one barrier per step a block may already reserve
+  // raster entries of step s while another still reads the count of step
+  // s - 1, so the offsets come from the step counts instead (a step's
+  // entries are contiguous: its reservations all follow the previous
+  // barrier).  After the last barrier every count is final; block 0 scans.
+  if (a.raster_cap && blockIdx.x == 0) {
+    const uint32_t per = (n_steps + kPersistBlock - 1) / kPersistBlock;
+    const uint32_t q0 = min(n_steps, threadIdx.x * per), q1 = min(n_steps, q0 + per);
+    uint32_t tot = 0;
+    for (uint32_t q = q0; q < q1; ++q)
+      for (uint32_t g = 0; g < a.n_segs; ++g) tot += __ldcg(a.counts + (size_t)q * a.n_segs + g);
+    uint32_t incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(kFull, incl, o);
+      if (lane >= (uint32_t)o) incl += v;
+    }
+    __syncthreads();  // s_wsum's last readers were in the prologue
+    if (lane == 31) s_wsum[wib] = incl;
+    __syncthreads();
+    if (wib == 0) {
+      const uint32_t x = s_wsum[lane];
+      uint32_t xi = x;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(kFull, xi, o);
+        if (lane >= (uint32_t)o) xi += v;
+      }
+      s_wsum[lane] = xi - x;
+    }
+    __syncthreads();
+    uint32_t run = s_wsum[wib] + incl - tot;
+    for (uint32_t q = q0; q < q1; ++q) {
+      for (uint32_t g = 0; g < a.n_segs; ++g) run += __ldcg(a.counts + (size_t)q * a.n_segs + g);
+      a.raster_off[q + 1] = run;
+    }
+  }
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
-    if (a.raster_cap) a.raster_off[n_steps] = __ldcg(&ctl->raster_count);
     ctl->step = t0 + n_steps;
     ctl->ring_slot = ix.slot;
     ctl->hist_row = ix.hrow;
