@@ -39,7 +39,7 @@ void sgb_config_init(sgb_config* cfg) {
 
 const char* sgb_last_error(void) { return last_error(); }
 
-int32_t sgb_abi_version(void) { return 1; }
+int32_t sgb_abi_version(void) { return 2; }
 
 int sgb_net_create(sgb_net** out) {
   if (!out) return set_error(SGB_ERR_ARG, "out is NULL");
@@ -318,6 +318,7 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
                           ? persistent_kernel_kind(s.args, s.persistent_blocks)
                           : SGB_KERNEL_GRAPH;
   info->push_smem_bytes = info->step_kernel == SGB_KERNEL_FUSED ? (int32_t)s.args.row_smem : 0;
+  info->shard_cells = info->step_kernel == SGB_KERNEL_FUSED ? s.n_shard_cells : 0;
   info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;
   info->weight_type = s.cfg.weight_type;

@@ -30,6 +30,12 @@ namespace sgb {
 constexpr int kBlock = 256;           // threads per block of the per-step kernels
 constexpr int kPersistBlock = 1024;   // threads per block of the persistent kernel
 constexpr uint32_t kPushChunk = 256;  // synapses per push work item (8 per lane)
+// Fused persistent kernel: a cell with at least kShardMin synapses of delay
+// >= 2 keeps only its delay-1 synapses; the rest is cut into shards of
+// kPushChunk synapses that other blocks push one step later (at most
+// kMaxShards per block).
+constexpr uint32_t kShardMin = 256;
+constexpr uint32_t kMaxShards = 128;
 constexpr uint32_t kPullUnit = 1024;  // ELL entries per dense-pull work unit (32 per lane)
 constexpr uint32_t kStdpUnit = 128;   // ELL cells per plasticity work unit (4 per lane)
 constexpr int kPullBlock = 1024;             // threads per k_pull block (one per SM)
@@ -163,6 +169,11 @@ struct StepArgs {
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer
   uint32_t row_smem;              // fused persistent kernel: shared-memory bytes for push rows (0: none)
+  uint32_t n_shards;              // fused persistent kernel: deferred shards (0: none)
+  uint32_t shard_grid;            // the grid size the shards were dealt for
+  const uint32_t* push_split;     // [n_pad] end of the part of a row its owner pushes (shards on)
+  const uint4* shards;            // {cell, first synapse, length, 0}, grouped by block
+  const uint32_t* shard_off;      // [shard_grid + 1] each block's range of shards
   int32_t bf16;
   int32_t substeps;
 };

@@ -59,6 +59,7 @@ Sim::~Sim() {
   if (d_push) cudaFree(d_push);
   if (d_misc) cudaFree(d_misc);
   if (d_plast) cudaFree(d_plast);
+  if (d_shard) cudaFree(d_shard);
   if (h_counts) cudaFreeHost(h_counts);
   if (h_raster) cudaFreeHost(h_raster);
   if (h_raster_off) cudaFreeHost(h_raster_off);
@@ -205,20 +206,27 @@ static int upload_modes(Sim& s) {
   std::vector<uint32_t> syn((size_t)total);
   std::vector<float> wf(s.bf16 ? 0 : (size_t)total);
   std::vector<uint16_t> wh(s.bf16 ? (size_t)total : 0);
+  // Each row holds its delay-1 synapses first (pass 0), then the others:
+  // split[c] is where the delay >= 2 part of cell c's row starts.
+  std::vector<uint32_t> split;
   {
     std::vector<uint32_t> fill(row.begin(), row.end() - 1);
-    for (size_t k = 0; k < s.projs.size(); ++k) {
-      if (s.projs[k].mode != SGB_PROP_CSR) continue;
-      const ProjTables& t = s.ptab[k];
-      const Projection& pr = s.nets[t.net].projs[t.proj];
-      const uint32_t pre_base = s.segs[t.pre_seg].base, post_base = s.segs[t.post_seg].base;
-      for (size_t i = 0; i < pr.pre_idx.size(); ++i) {
-        const uint32_t q = fill[pre_base + pr.pre_idx[i]]++;
-        syn[q] = (post_base + pr.post_idx[i]) | ((uint32_t)pr.delay[i] << kPushPostBits) |
-                 ((uint32_t)pr.channel << 31);
-        const float w = scaled_weight(pr.weight[i], t.scale_bits, s.bf16);
-        if (s.bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (size_t k = 0; k < s.projs.size(); ++k) {
+        if (s.projs[k].mode != SGB_PROP_CSR) continue;
+        const ProjTables& t = s.ptab[k];
+        const Projection& pr = s.nets[t.net].projs[t.proj];
+        const uint32_t pre_base = s.segs[t.pre_seg].base, post_base = s.segs[t.post_seg].base;
+        for (size_t i = 0; i < pr.pre_idx.size(); ++i) {
+          if ((pr.delay[i] == 1) != (pass == 0)) continue;
+          const uint32_t q = fill[pre_base + pr.pre_idx[i]]++;
+          syn[q] = (post_base + pr.post_idx[i]) | ((uint32_t)pr.delay[i] << kPushPostBits) |
+                   ((uint32_t)pr.channel << 31);
+          const float w = scaled_weight(pr.weight[i], t.scale_bits, s.bf16);
+          if (s.bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
+        }
       }
+      if (pass == 0) split = fill;
     }
   }
   const size_t wsz = s.bf16 ? 2 : 4;
@@ -244,16 +252,72 @@ static int upload_modes(Sim& s) {
     SGB_CUDA(cudaMemcpy((void*)a.pull_units, units.data(), units.size() * sizeof(PullUnit), cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
   a.n_pull_units = (uint32_t)units.size();
-  // Fused persistent kernel: shared memory for the push rows of the block
-  // holding the most synapses (word slot ws runs in block ws mod blocks).
+  // Fused persistent kernel.  Shards: the delay >= 2 parts of long rows
+  // (longest first) are cut into kPushChunk-synapse shards dealt round-robin
+  // over the blocks, so one spike's pushes spread over many SMs; a cell whose
+  // shards no longer fit keeps its whole row.  Then shared memory for the
+  // push rows of the block holding the most synapses (word slot ws runs in
+  // block ws mod blocks; a sharded cell's own part is its delay-1 synapses).
   a.row_smem = 0;
-  if (total > 0 && s.persistent_blocks > 0 &&
-      persistent_kernel_kind(a, s.persistent_blocks) == SGB_KERNEL_FUSED) {
+  a.n_shards = 0;
+  s.n_shard_cells = 0;
+  const bool fused = total > 0 && s.persistent_blocks > 0 &&
+                     persistent_kernel_kind(a, s.persistent_blocks) == SGB_KERNEL_FUSED;
+  std::vector<uint32_t> own_end(row.begin() + 1, row.end());
+  std::vector<std::vector<uint4>> blk_sh(fused && s.d_shard ? (size_t)s.persistent_blocks : 0);
+  if (!blk_sh.empty()) {
+    const uint32_t B = (uint32_t)blk_sh.size();
+    std::vector<uint32_t> cand;
+    for (uint32_t c = 0; c < s.n_pad; ++c)
+      if (row[c + 1] - split[c] >= kShardMin) cand.push_back(c);
+    std::stable_sort(cand.begin(), cand.end(), [&](uint32_t x, uint32_t y) {
+      return row[x + 1] - split[x] > row[y + 1] - split[y];
+    });
+    uint32_t cursor = 0;
+    for (uint32_t c : cand) {
+      std::vector<uint32_t> picked;
+      for (uint32_t q = split[c]; q < row[c + 1]; q += kPushChunk) {
+        uint32_t tries = 0;
+        while (tries < B && blk_sh[cursor].size() >= kMaxShards) { cursor = (cursor + 1) % B; ++tries; }
+        if (tries == B) break;
+        blk_sh[cursor].push_back(make_uint4(c, q, std::min(kPushChunk, row[c + 1] - q), 0u));
+        picked.push_back(cursor);
+        cursor = (cursor + 1) % B;
+      }
+      if ((uint64_t)picked.size() * kPushChunk < row[c + 1] - split[c]) {
+        for (uint32_t b : picked) blk_sh[b].pop_back();
+        break;
+      }
+      own_end[c] = split[c];
+      ++s.n_shard_cells;
+    }
+    std::vector<uint4> flat;
+    std::vector<uint32_t> off(B + 1, 0);
+    for (uint32_t b = 0; b < B; ++b) {
+      flat.insert(flat.end(), blk_sh[b].begin(), blk_sh[b].end());
+      off[b + 1] = (uint32_t)flat.size();
+    }
+    char* sb = (char*)s.d_shard;
+    const size_t o_sh = align_up((size_t)s.n_pad * 4, 256);
+    const size_t o_off = o_sh + align_up((size_t)B * kMaxShards * sizeof(uint4), 256);
+    SGB_CUDA(cudaMemcpy(sb, own_end.data(), (size_t)s.n_pad * 4, cudaMemcpyHostToDevice));
+    if (!flat.empty())
+      SGB_CUDA(cudaMemcpy(sb + o_sh, flat.data(), flat.size() * sizeof(uint4), cudaMemcpyHostToDevice));
+    SGB_CUDA(cudaMemcpy(sb + o_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice));
+    a.push_split = (const uint32_t*)sb;
+    a.shards = (const uint4*)(sb + o_sh);
+    a.shard_off = (const uint32_t*)(sb + o_off);
+    a.shard_grid = B;
+    a.n_shards = (uint32_t)flat.size();
+  }
+  if (fused) {
     std::vector<uint64_t> need((size_t)s.persistent_blocks, 0);
     for (size_t ws = 0; ws < s.upd_words.size(); ++ws) {
       const uint32_t w = s.upd_words[ws];
-      need[ws % need.size()] += row[(size_t)w * 32 + 32] - row[(size_t)w * 32];
+      for (uint32_t c = w * 32; c < w * 32 + 32; ++c) need[ws % need.size()] += own_end[c] - row[c];
     }
+    for (size_t b = 0; b < blk_sh.size(); ++b)
+      for (const uint4& h : blk_sh[b]) need[b] += h.z;
     const uint64_t most = *std::max_element(need.begin(), need.end()) * sizeof(uint2);
     const uint64_t bytes = std::min<uint64_t>((most + 255) & ~255ull, fused_row_smem_max());
     if (bytes >= 1024) {
@@ -692,6 +756,14 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   if (!upd_words.empty())
     SGB_CUDA(cudaMemcpy((void*)a.upd_words, upd_words.data(), upd_words.size() * 4, cudaMemcpyHostToDevice));
   s.upd_words = upd_words;
+  if ((uint64_t)upd_words.size() * 32 <= (uint64_t)s.persistent_blocks * kPersistBlock) {
+    // Resident networks may run the fused kernel: room for its shards.
+    const size_t bytes = align_up((size_t)s.n_pad * 4, 256) +
+                         align_up((size_t)s.persistent_blocks * kMaxShards * sizeof(uint4), 256) +
+                         ((size_t)s.persistent_blocks + 1) * 4;
+    SGB_CUDA(cudaMalloc(&s.d_shard, bytes));
+    s.push_bytes += bytes;
+  }
   int rc = upload_modes(s);
   if (rc) return rc;
 

@@ -65,8 +65,10 @@ struct Sim {
   size_t hist_bytes = 0;      // spike history + its summary
   int persistent_blocks = 0;
   std::vector<uint32_t> upd_words;  // host copy of args.upd_words
+  int64_t n_shard_cells = 0;        // cells whose delay >= 2 synapses are sharded
   // Plasticity (STDP) of plastic projections.
   void* d_plast = nullptr;
+  void* d_shard = nullptr;    // fused-kernel shards: split points, shard list, per-block offsets
   size_t off_recent = 0;      // per-cell spike registers inside d_plast
   std::vector<PlastHost> plast;
   // Persisting L2 window over the cell state (su, sg).

@@ -931,12 +931,24 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
 // memory), so a step's pushes read no global memory.
 constexpr uint32_t kBlockItems = 2048;  // push items per block and step (16 KiB)
 
+// An item of the fused kernel: (first synapse, length << 23 | flags); flag 1:
+// the synapses are in the block's shared-memory rows, flag 2: a shard of the
+// previous step's spike (its delays count from that step's ring slot).
+template <bool BF16>
+__device__ __forceinline__ uint32_t push_any(const StepArgs& a, const uint2* rows, uint2 it,
+                                             uint32_t slot, uint32_t prev) {
+  const uint32_t s0 = (it.y & 2u) ? prev : slot;
+  return (it.y & 1u) ? push_item_smem(a, rows, it, s0) : push_item<BF16>(a, it, s0);
+}
+
 template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs a,
                                                                        uint32_t n_steps) {
   __shared__ uint2 s_items[kBlockItems];
   __shared__ uint32_t s_n[2];  // item count of step parity p; the other one is reset
   __shared__ uint32_t s_wsum[kPersistBlock / 32];
+  __shared__ uint4 s_sh[kMaxShards];  // {cell, first synapse, length << 23 | flags, global first}
+  __shared__ uint32_t s_shtot;
   extern __shared__ uint2 s_rows[];
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
@@ -971,6 +983,38 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       r1 = __ldg(a.push_row + i + 1);
     }
   }
+  // Shards: a sharded cell pushes only its delay-1 synapses (r1 becomes its
+  // split point); the rest of its row is cut into shards dealt to blocks,
+  // which push a shard in the step after the cell's spike, reading the spike
+  // from the history.  Its delays d >= 2 count from the spike's ring slot, so
+  // the targets t - 1 + d are still ahead of the update that reads slot t.
+  // This block's n_sh shards go first into shared memory while they fit.
+  const bool sharded = a.n_shards != 0 && gridDim.x == a.shard_grid;
+  uint32_t n_sh = 0;
+  if (sharded) {
+    if (valid) r1 = __ldg(a.push_split + i);
+    const uint32_t h0 = __ldg(a.shard_off + blockIdx.x);
+    n_sh = __ldg(a.shard_off + blockIdx.x + 1) - h0;
+    if (threadIdx.x == 0) {
+      const uint32_t cap = a.row_smem / (uint32_t)sizeof(uint2);
+      uint32_t used = 0;
+      for (uint32_t j = 0; j < n_sh; ++j) {
+        const uint4 h = a.shards[h0 + j];
+        const bool in = h.z <= cap - used;
+        s_sh[j] = make_uint4(h.x, in ? used : h.y, (h.z << 23) | (in ? 3u : 2u), h.y);
+        if (in) used += h.z;
+      }
+      s_shtot = used;
+    }
+    __syncthreads();
+    for (uint32_t j = wib; j < n_sh; j += kPersistBlock / 32) {
+      const uint4 h = s_sh[j];
+      if (h.z & 1u)
+        for (uint32_t k = lane; k < (h.z >> 23); k += 32)
+          s_rows[h.y + k] = make_uint2(__ldg(a.push_syn + h.w + k),
+                                       (uint32_t)__float2int_rn(load_weight<BF16>(a.push_w, h.w + k)));
+    }
+  }
   // Input cells: the stimulus decision of the coming step, drawn ahead (it
   // depends only on the step index) -- for later steps while the previous
   // grid barrier completes.
@@ -999,7 +1043,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       s_wsum[lane] = xi - x;
     }
     __syncthreads();
-    const uint32_t base = s_wsum[wib] + incl - len;
+    const uint32_t base = (sharded ? s_shtot : 0u) + s_wsum[wib] + incl - len;
     const uint32_t cap = a.row_smem / (uint32_t)sizeof(uint2);
     if (len && base <= cap && len <= cap - base) sb = base;
     uint32_t todo = __ballot_sync(kFull, sb != kNoRow);
@@ -1015,6 +1059,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   }
   unsigned long long target = 0;
   uint32_t walked = 0;
+  bool aborted = false;
   if (threadIdx.x == 0) s_n[0] = s_n[1] = 0;
   __syncthreads();
   for (uint32_t s = 0; s < n_steps; ++s) {
@@ -1022,6 +1067,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     ix.rel = s;
     const uint32_t par = s & 1u;
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
+    // Shards of the previous step's spikes (none at a launch's first step:
+    // each launch pushes its last step's shards itself, after the loop).
+    const bool sh_ck = s > 0 && threadIdx.x < n_sh;
+    const uint32_t sh_w =
+        sh_ck ? __ldcg(hist_base(a, ix.hrow) + a.n_words + (s_sh[threadIdx.x].x >> 5)) : 0u;
     uint32_t off = 0, nit = 0;
     if (has) {
       const bool fired = lif ? cell_fire(a, a.segs[seg], i, 0u, valid, st, 0u, ix) : next_in;
@@ -1063,15 +1113,21 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         }
       }
     }
+    bool sh_spill = false;
+    if (sh_ck) {
+      const uint4 h = s_sh[threadIdx.x];
+      if ((sh_w >> (h.x & 31u)) & 1u) {
+        const uint32_t o = atomicAdd(&s_n[par], 1u);
+        if (o < kBlockItems) s_items[o] = make_uint2(h.y, h.z); else sh_spill = true;
+      }
+    }
     __syncthreads();
     const uint32_t n_items = min(s_n[par], kBlockItems);
     // The other parity's count was last read before this step's __syncthreads.
     if (threadIdx.x == 0) s_n[par ^ 1u] = 0;
-    for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32) {
-      const uint2 it = s_items[u];
-      walked += (it.y & 1u) ? push_item_smem(a, s_rows, it, ix.slot)
-                            : push_item<BF16>(a, it, ix.slot);
-    }
+    const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
+    for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32)
+      walked += push_any<BF16>(a, s_rows, s_items[u], ix.slot, prev);
     // Items beyond the block's capacity are delivered by the warp that made them.
     uint32_t spill = __ballot_sync(kFull, off + nit > kBlockItems);
     while (spill) {
@@ -1084,15 +1140,43 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         walked += push_item<BF16>(a, make_uint2(q0, min(kPushChunk, b1 - q0) << 23), ix.slot);
       }
     }
+    if (n_sh) {
+      uint32_t sp = __ballot_sync(kFull, sh_spill);
+      while (sp) {
+        const int src = __ffs(sp) - 1;
+        sp &= sp - 1;
+        const uint4 h = s_sh[wib * 32u + src];
+        walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
+      }
+    }
     grid_arrive(a, target);
     if (stim && s + 1 < n_steps)
       next_in = input_fire(a, a.segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1);
-    if (!grid_wait(a, target)) break;
+    if (!grid_wait(a, target)) {
+      aborted = true;
+      break;
+    }
     ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
     ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
   }
   if (valid && lif) state_out(a, i, st);
+  // The shards of the last step's spikes (ix has advanced past that step).
+  if (!aborted && n_sh && n_steps) {
+    const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
+    bool hit = false;
+    if (threadIdx.x < n_sh) {
+      const uint32_t c = s_sh[threadIdx.x].x;
+      hit = (__ldcg(hist_base(a, ix.hrow) + a.n_words + (c >> 5)) >> (c & 31u)) & 1u;
+    }
+    uint32_t sp = __ballot_sync(kFull, hit);
+    while (sp) {
+      const int src = __ffs(sp) - 1;
+      sp &= sp - 1;
+      const uint4 h = s_sh[wib * 32u + src];
+      walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
+    }
+  }
   // Raster offsets: with one barrier per step a block may already reserve
   // raster entries of step s while another still reads the count of step
   // s - 1, so the offsets come from the step counts instead (a step's

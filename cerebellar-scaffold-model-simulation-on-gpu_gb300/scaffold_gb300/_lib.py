@@ -85,7 +85,8 @@ class SimInfo(C.Structure):
                 ("weight_type", C.c_int32), ("substeps", C.c_int32), ("chunk_steps", C.c_int32),
                 ("dt_ms", C.c_double), ("events", C.c_int64), ("delivered", C.c_int64),
                 ("step_kernel", C.c_int32), ("push_smem_bytes", C.c_int32), ("pulled", C.c_int64),
-                ("pull_entries", C.c_int64), ("l2_persist_bytes", C.c_int64)]
+                ("pull_entries", C.c_int64), ("l2_persist_bytes", C.c_int64),
+                ("shard_cells", C.c_int64)]
 
 
 P = C.POINTER

@@ -169,6 +169,7 @@ typedef struct sgb_sim_info {
   int64_t pulled;        /* dense-pull entries whose pre cell had spiked (deliveries) since the last reset */
   int64_t pull_entries;  /* dense-table entries streamed per step (0 without dense projections) */
   int64_t l2_persist_bytes; /* L2 set aside for the persisting state window (0: none)   */
+  int64_t shard_cells;   /* SGB_KERNEL_FUSED: cells whose delay >= 2 synapses other blocks push */
 } sgb_sim_info;
 
 /* Step kernels (sgb_sim_info.step_kernel). */

@@ -250,8 +250,27 @@ def test_fused_kernel_rows_partly_in_shared_memory(weight):
     info = sim.info()
     assert info.step_kernel == 3  # SGB_KERNEL_FUSED
     assert 0 < info.push_smem_bytes < 32000 * 8
+    assert info.shard_cells > 0   # ~750 synapses of delay >= 2 per cell
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 5, steps, bf16=weight == sg.WEIGHT_BF16)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
     assert counts[:, 1].sum() > 0
+    sim.close()
+
+
+@pytest.mark.parametrize("chunk", [97, 1000])
+def test_config2_fused_shards_bit_exact(chunk):
+    """Config 2 (92,550 cells) in the fused persistent kernel: the Golgi cells'
+    1,600-synapse rows keep their delay-1 synapses and hand the rest, as
+    256-synapse shards, to other blocks one step later; short chunks check
+    that every launch pushes its last step's shards before it ends."""
+    net = sg.scaffold(2, 1.0, 3)
+    steps = 400
+    sim = sg.Simulation([net], [3], exec_mode=sg.EXEC_PERSISTENT, raster=True, chunk_steps=chunk)
+    info = sim.info()
+    assert info.step_kernel == 3 and info.shard_cells >= 200
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
+    exp = _oracle(net, 3, steps)
+    _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    assert sim.info().delivered == exp[6]
     sim.close()
