@@ -159,6 +159,7 @@ struct StepArgs {
   double* totals;                 // [n_segs]
   unsigned long long* bar;        // grid-barrier arrival counter (zeroed per launch)
   uint32_t n_pad, n_words, n_segs, n_projs;
+  uint32_t n_srcs;                // stimulus sources (all segments)
   uint32_t ring_slots, hist_rows;
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;

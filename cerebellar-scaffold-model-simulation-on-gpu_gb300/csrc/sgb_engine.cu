@@ -629,6 +629,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.n_pad = s.n_pad;
   a.n_words = s.n_words;
   a.n_segs = (uint32_t)nseg;
+  a.n_srcs = (uint32_t)s.srcs.size();
   a.n_projs = (uint32_t)s.projs.size();
   a.ring_slots = s.ring_slots;
   a.hist_rows = s.hist_rows;

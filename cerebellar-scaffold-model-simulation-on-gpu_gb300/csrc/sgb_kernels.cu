@@ -50,8 +50,12 @@ __device__ __forceinline__ bool window_on(const SrcDev& s, int64_t k) {
   if (s.win_end <= s.win_start) return true;
   int64_t kk = k;
   if (s.win_period > 0) {
-    kk = k % s.win_period;
-    if (kk < 0) kk += s.win_period;
+    if ((uint64_t)k <= 0xFFFFFFFFull && (uint64_t)s.win_period <= 0xFFFFFFFFull) {
+      kk = (int64_t)((uint32_t)k % (uint32_t)s.win_period);  // same value, 32-bit divide
+    } else {
+      kk = k % s.win_period;
+      if (kk < 0) kk += s.win_period;
+    }
   }
   return kk >= s.win_start && kk < s.win_end;
 }
@@ -64,8 +68,8 @@ __device__ __forceinline__ bool periodic_fire(const SrcDev& s, int64_t k) {
   return floor(x1) != floor(x0);
 }
 
-__device__ bool input_fire(const StepArgs& a, const SegDev& sd, uint32_t local, uint32_t mask,
-                           unsigned long long t) {
+__device__ bool input_fire(const StepArgs& a, const SrcDev* srcs, const SegDev& sd, uint32_t local,
+                           uint32_t mask, unsigned long long t) {
   bool fire = false;
   U4 r{};
   for (int s = 0; s < a.substeps; ++s) {
@@ -76,7 +80,7 @@ __device__ bool input_fire(const StepArgs& a, const SegDev& sd, uint32_t local, 
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;
-      const SrcDev src = a.srcs[sd.src_first + b];
+      const SrcDev src = srcs[sd.src_first + b];
       if (!window_on(src, k)) continue;
       if (src.kind == SGB_INPUT_POISSON)
         fire |= (uint64_t)x < src.thresh;
@@ -159,7 +163,7 @@ __device__ __forceinline__ bool cell_fire(const StepArgs& a, const SegDev& sd, u
                                           uint32_t local, bool valid, float4& st, uint32_t mask,
                                           const StepIdx& ix) {
   if (!valid) return false;
-  if (sd.kind == kSegInput) return mask ? input_fire(a, sd, local, mask, ix.t) : false;
+  if (sd.kind == kSegInput) return mask ? input_fire(a, a.srcs, sd, local, mask, ix.t) : false;
   int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i;
   const int2 acc = __ldcg(rp);
   if (acc.x | acc.y) __stcg(rp, make_int2(0, 0));
@@ -258,7 +262,7 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
   if (valid) {
     if (sd.kind == kSegInput) {
       const uint32_t mask = __ldg(a.src_mask + i);
-      if (mask) fired = input_fire(a, sd, local, mask, ix.t);
+      if (mask) fired = input_fire(a, a.srcs, sd, local, mask, ix.t);
     } else {
       if (in.acc.x | in.acc.y)
         __stcg(reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i, make_int2(0, 0));
@@ -787,9 +791,10 @@ __device__ __forceinline__ void grid_arrive(const StepArgs& a, unsigned long lon
     asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
 }
 
-__device__ __forceinline__ bool grid_wait(const StepArgs& a, unsigned long long target) {
+__device__ __forceinline__ bool grid_wait(const StepArgs& a, unsigned long long target,
+                                          uint32_t poller = 0) {
   __shared__ int abort_flag;
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == poller) {
     int ok = 1;
     const unsigned long long want = target + a.bar_extra;
     unsigned long long t0 = 0;
@@ -949,7 +954,18 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   __shared__ uint32_t s_wsum[kPersistBlock / 32];
   __shared__ uint4 s_sh[kMaxShards];  // {cell, first synapse, length << 23 | flags, global first}
   __shared__ uint32_t s_shtot;
+  __shared__ uint32_t s_od[kPersistBlock];  // out-degree of each thread's cell
+  // Segment descriptors and stimulus sources, read every step, in shared
+  // memory (when few enough): a miss in the small L1 that this kernel's
+  // shared-memory carve-out leaves would cost an L2 round trip per step.
+  constexpr uint32_t kSegCache = 16, kSrcCache = 16;
+  __shared__ SegDev s_seg[kSegCache];
+  __shared__ SrcDev s_src[kSrcCache];
   extern __shared__ uint2 s_rows[];
+  const SegDev* segs = a.n_segs <= kSegCache ? s_seg : a.segs;
+  const SrcDev* srcs = a.n_srcs <= kSrcCache ? s_src : a.srcs;
+  if (a.n_segs <= kSegCache && threadIdx.x < a.n_segs) s_seg[threadIdx.x] = a.segs[threadIdx.x];
+  if (a.n_srcs <= kSrcCache && threadIdx.x < a.n_srcs) s_src[threadIdx.x] = a.srcs[threadIdx.x];
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -962,7 +978,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   const bool has = ws < a.n_upd_words;
   // st: a LIF cell's state {u, g0, g1, ref}; an input cell's source mask and
   // index within its segment (bits of st.x, st.y).
-  uint32_t w = 0, seg = 0, i = 0, r0 = 0, r1 = 0, od = 0;
+  uint32_t w = 0, seg = 0, i = 0, r0 = 0, r1 = 0;
+  s_od[threadIdx.x] = 0;
   bool valid = false, lif = false;
   float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
   if (has) {
@@ -978,7 +995,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         st = state_in(a.su[i], a.sg[i], sd.Vr);
       else
         st = make_float4(__uint_as_float(__ldg(a.src_mask + i)), __uint_as_float(local), 0.f, 0.f);
-      od = __ldg(a.outdeg + i);
+      s_od[threadIdx.x] = __ldg(a.outdeg + i);
       r0 = __ldg(a.push_row + i);
       r1 = __ldg(a.push_row + i + 1);
     }
@@ -1019,12 +1036,19 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   // depends only on the step index) -- for later steps while the previous
   // grid barrier completes.
   const bool stim = valid && !lif && __float_as_uint(st.x) != 0u;
-  bool next_in = stim && input_fire(a, a.segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), t0);
+  // The barrier is polled from the highest warp without stimulated cells, so
+  // the poll starts as soon as the block has arrived.
+  __shared__ uint32_t s_poller;
+  if (threadIdx.x == 0) s_poller = 0;
+  __syncthreads();  // also publishes s_seg / s_src
+  bool next_in = stim && input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), t0);
+  const bool warp_stim = __any_sync(kFull, stim);
+  if (lane == 0 && !warp_stim) atomicMax(&s_poller, threadIdx.x);
   // Push rows into shared memory: sb = the row's offset there, or kNoRow.
   constexpr uint32_t kNoRow = 0xFFFFFFFFu;
   uint32_t sb = kNoRow;
+  const uint32_t len = r1 - r0;
   if (a.row_smem) {
-    const uint32_t len = r1 - r0;
     uint32_t incl = len;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -1057,6 +1081,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
                                     (uint32_t)__float2int_rn(load_weight<BF16>(a.push_w, q0 + k)));
     }
   }
+  // From here a row is (qb, rl): its first synapse in shared or global
+  // memory and its length, with bit 31 set when it is in shared memory.
+  const uint32_t qb = sb != kNoRow ? sb : r0;
+  const uint32_t rl = len | (sb != kNoRow ? 0x80000000u : 0u);
   unsigned long long target = 0;
   uint32_t walked = 0;
   bool aborted = false;
@@ -1074,14 +1102,14 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         sh_ck ? __ldcg(hist_base(a, ix.hrow) + a.n_words + (s_sh[threadIdx.x].x >> 5)) : 0u;
     uint32_t off = 0, nit = 0;
     if (has) {
-      const bool fired = lif ? cell_fire(a, a.segs[seg], i, 0u, valid, st, 0u, ix) : next_in;
+      const bool fired = lif ? cell_fire(a, segs[seg], i, 0u, valid, st, 0u, ix) : next_in;
       const uint32_t ballot = __ballot_sync(kFull, fired);
       if (lane == 0) put_hist(a, ix, w, ballot);
       if (ballot) {
         const uint32_t n = __popc(ballot);
         const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
-        const uint32_t ev = __reduce_add_sync(kFull, fired ? od : 0u);
-        nit = fired ? (r1 - r0 + kPushChunk - 1) / kPushChunk : 0u;
+        const uint32_t ev = __reduce_add_sync(kFull, fired ? s_od[threadIdx.x] : 0u);
+        nit = fired ? ((rl & 0x7FFFFFFFu) + kPushChunk - 1) / kPushChunk : 0u;
         uint32_t incl = nit;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1097,10 +1125,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
           if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
         }
         off = __shfl_sync(kFull, off, 0) + incl - nit;
-        // Item: (first synapse, length << 23 | 1 when the row is in shared memory).
         for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
-          const uint32_t q = k * kPushChunk, len = min(kPushChunk, r1 - r0 - q) << 23;
-          s_items[off + k] = sb != kNoRow ? make_uint2(sb + q, len | 1u) : make_uint2(r0 + q, len);
+          const uint32_t q = k * kPushChunk;
+          s_items[off + k] = make_uint2(qb + q, (min(kPushChunk, (rl & 0x7FFFFFFFu) - q) << 23) |
+                                                    (rl >> 31));
         }
         if (a.raster_cap) {
           roff = __shfl_sync(kFull, roff, 0);
@@ -1134,10 +1162,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       const int src = __ffs(spill) - 1;
       spill &= spill - 1;
       const uint32_t o = __shfl_sync(kFull, off, src), c = __shfl_sync(kFull, nit, src);
-      const uint32_t b0 = __shfl_sync(kFull, r0, src), b1 = __shfl_sync(kFull, r1, src);
+      const uint32_t b0 = __shfl_sync(kFull, qb, src), bl = __shfl_sync(kFull, rl, src);
       for (uint32_t k = o < kBlockItems ? kBlockItems - o : 0; k < c; ++k) {
-        const uint32_t q0 = b0 + k * kPushChunk;
-        walked += push_item<BF16>(a, make_uint2(q0, min(kPushChunk, b1 - q0) << 23), ix.slot);
+        const uint32_t q = k * kPushChunk;
+        const uint2 it = make_uint2(b0 + q, (min(kPushChunk, (bl & 0x7FFFFFFFu) - q) << 23) | (bl >> 31));
+        walked += push_any<BF16>(a, s_rows, it, ix.slot, prev);
       }
     }
     if (n_sh) {
@@ -1151,8 +1180,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     }
     grid_arrive(a, target);
     if (stim && s + 1 < n_steps)
-      next_in = input_fire(a, a.segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1);
-    if (!grid_wait(a, target)) {
+      next_in = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1);
+    if (!grid_wait(a, target, s_poller)) {
       aborted = true;
       break;
     }
