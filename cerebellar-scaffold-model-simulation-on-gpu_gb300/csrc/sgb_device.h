@@ -50,24 +50,30 @@ constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;  // grid-barrier
 
 enum SegKind : uint32_t { kSegLif = 0, kSegInput = 1 };
 
-struct SegDev {
+// 16-byte groups: the header and the four groups of LIF constants from El to
+// sel are fetched with vector loads.
+struct alignas(16) SegDev {
   uint32_t base;       // padded index of cell 0 (multiple of 32)
   uint32_t count;      // cells
   uint32_t key_base;   // Philox neuron id of cell 0 (instance-local, unpadded)
   uint32_t kind;       // SegKind
-  uint64_t seed;       // instance seed
-  uint32_t src_first, src_count;  // stimulus sources (INPUT segments)
-  uint32_t out_first, out_count;  // outgoing projections (index list)
   float El, Vr, Vth, Ie;
   float neg_gL, dt_cm;            // -gL, dt/Cm
   float keep[2];                  // 1 - dt/tau_c
   float gw[2];                    // g_bar_c * w_c
   float E[2];
   float inv_scale[2];             // 2^-S of the exc / inh accumulators
+  uint32_t sel[2];                // accumulator feeding channel c (0 exc, 1 inh)
   int32_t ref_steps;              // (int)(dt_ref / dt), computed in double
   int32_t substeps;
-  uint32_t sel[2];                // accumulator feeding channel c (0 exc, 1 inh)
+  uint64_t seed;       // instance seed
+  uint32_t src_first, src_count;  // stimulus sources (INPUT segments)
+  uint32_t out_first, out_count;  // outgoing projections (index list)
 };
+static_assert(offsetof(SegDev, El) == 16 && offsetof(SegDev, neg_gL) == 32 &&
+                  offsetof(SegDev, gw) == 48 && offsetof(SegDev, inv_scale) == 64 &&
+                  offsetof(SegDev, ref_steps) == 80,
+              "SegDev vector groups");
 
 struct ProjDev {
   uint32_t pre_base, post_base;   // padded segment bases

@@ -97,33 +97,59 @@ __device__ bool input_fire(const StepArgs& a, const SrcDev* srcs, const SegDev& 
 // only, spike test on the old potential, refractory count, reset.  Every
 // operation is a single IEEE-rounded FP32 op so a CPU restatement reproduces
 // it bit for bit.
-__device__ __forceinline__ bool lif_update(const SegDev& sd, int substeps, float4& st, int2 acc) {
+// The LIF constants of a segment, fetched as four 16-byte groups (plus the
+// refractory length): a word's update issues 5 loads for them, not 17.
+struct LifK {
+  float El, Vr, Vth, Ie, neg_gL, dt_cm, keep0, keep1, gw0, gw1, E0, E1, inv0, inv1;
+  uint32_t sel0, sel1;
+  int32_t ref_steps;
+};
+__device__ __forceinline__ LifK lif_k(const SegDev& sd) {
+  const float4* p = reinterpret_cast<const float4*>(&sd.El);
+  const float4 a = p[0], b = p[1], c = p[2], d = p[3];
+  LifK k;
+  k.El = a.x; k.Vr = a.y; k.Vth = a.z; k.Ie = a.w;
+  k.neg_gL = b.x; k.dt_cm = b.y; k.keep0 = b.z; k.keep1 = b.w;
+  k.gw0 = c.x; k.gw1 = c.y; k.E0 = c.z; k.E1 = c.w;
+  k.inv0 = d.x; k.inv1 = d.y; k.sel0 = __float_as_uint(d.z); k.sel1 = __float_as_uint(d.w);
+  k.ref_steps = sd.ref_steps;
+  return k;
+}
+
+// SUB = 1: the single-substep form of the same operations (the benchmark
+// configurations); SUB = 0: `substeps` substeps.
+template <int SUB>
+__device__ __forceinline__ bool lif_update(const LifK& k, int substeps, float4& st, int2 acc) {
   float u = st.x, g0 = st.y, g1 = st.z;
   int ref = __float_as_int(st.w);
-  const float dge = __fmul_rn(__int2float_rn(acc.x), sd.inv_scale[0]);
-  const float dgi = __fmul_rn(__int2float_rn(acc.y), sd.inv_scale[1]);
-  const float in0 = sd.sel[0] ? dgi : dge;
-  const float in1 = sd.sel[1] ? dgi : dge;
+  const float dge = __fmul_rn(__int2float_rn(acc.x), k.inv0);
+  const float dgi = __fmul_rn(__int2float_rn(acc.y), k.inv1);
+  const float in0 = k.sel0 ? dgi : dge;
+  const float in1 = k.sel1 ? dgi : dge;
   bool spk = false;
-  for (int s = 0; s < substeps; ++s) {
-    const float isyn =
-        __fmaf_rn(g1, __fsub_rn(u, sd.E[1]), __fmul_rn(g0, __fsub_rn(u, sd.E[0])));
-    const float cur = __fsub_rn(__fmaf_rn(sd.neg_gL, __fsub_rn(u, sd.El), sd.Ie), isyn);
-    const float du = __fmul_rn(sd.dt_cm, cur);
+  const int n = SUB == 1 ? 1 : substeps;
+  for (int s = 0; s < n; ++s) {
+    const float isyn = __fmaf_rn(g1, __fsub_rn(u, k.E1), __fmul_rn(g0, __fsub_rn(u, k.E0)));
+    const float cur = __fsub_rn(__fmaf_rn(k.neg_gL, __fsub_rn(u, k.El), k.Ie), isyn);
+    const float du = __fmul_rn(k.dt_cm, cur);
     if (s == 0) {
-      g0 = __fmaf_rn(g0, sd.keep[0], __fmul_rn(sd.gw[0], in0));
-      g1 = __fmaf_rn(g1, sd.keep[1], __fmul_rn(sd.gw[1], in1));
+      g0 = __fmaf_rn(g0, k.keep0, __fmul_rn(k.gw0, in0));
+      g1 = __fmaf_rn(g1, k.keep1, __fmul_rn(k.gw1, in1));
     } else {
-      g0 = __fmul_rn(g0, sd.keep[0]);
-      g1 = __fmul_rn(g1, sd.keep[1]);
+      g0 = __fmul_rn(g0, k.keep0);
+      g1 = __fmul_rn(g1, k.keep1);
     }
-    const bool above = u > sd.Vth;
+    const bool above = u > k.Vth;
     spk |= above;
-    ref = above ? sd.ref_steps : (ref > 0 ? ref - 1 : 0);
-    u = ref ? sd.Vr : __fadd_rn(u, du);
+    ref = above ? k.ref_steps : (ref > 0 ? ref - 1 : 0);
+    u = ref ? k.Vr : __fadd_rn(u, du);
   }
   st = make_float4(u, g0, g1, __int_as_float(ref));
   return spk;
+}
+
+__device__ __forceinline__ bool lif_step(const LifK& k, int substeps, float4& st, int2 acc) {
+  return substeps == 1 ? lif_update<1>(k, 1, st, acc) : lif_update<0>(k, substeps, st, acc);
 }
 
 // ---- phase 1: one warp updates the 32 cells of word w --------------------------
@@ -167,7 +193,7 @@ __device__ __forceinline__ bool cell_fire(const StepArgs& a, const SegDev& sd, u
   int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i;
   const int2 acc = __ldcg(rp);
   if (acc.x | acc.y) __stcg(rp, make_int2(0, 0));
-  return lif_update(sd, a.substeps, st, acc);
+  return lif_step(lif_k(sd), a.substeps, st, acc);
 }
 
 // Spike bookkeeping of one word: bitmap word, per-segment count, event count,
@@ -266,8 +292,9 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
     } else {
       if (in.acc.x | in.acc.y)
         __stcg(reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i, make_int2(0, 0));
-      float4 st = state_in(in.u, in.g, sd.Vr);
-      fired = lif_update(sd, a.substeps, st, in.acc);
+      const LifK k = lif_k(sd);
+      float4 st = state_in(in.u, in.g, k.Vr);
+      fired = lif_step(k, a.substeps, st, in.acc);
       state_out(a, i, st);
     }
     // Handles with plastic projections (per-step drivers only): each cell's
