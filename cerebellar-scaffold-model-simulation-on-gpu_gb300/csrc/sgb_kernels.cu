@@ -38,6 +38,11 @@ struct StepIdx {
   uint32_t hrow;  // t % hist_rows
   uint32_t srow;  // t % (hist_rows + 1): spike-summary row
   uint32_t rel;   // step index within the chunk
+  // Element offsets of the step's rows, computed once per step (all fit 32
+  // bits: ring_slots * n_pad < 2^31, 2 * hist_rows * n_words <= 2^28).
+  uint32_t roff;   // ring slot: slot * n_pad (int2 elements)
+  uint32_t hoff;   // history row of step t: (hist_rows - 1 - hrow) * n_words
+  uint32_t hoff2;  // its second copy, hist_rows rows further
 };
 
 template <bool BF16>
@@ -168,9 +173,8 @@ __device__ __forceinline__ uint32_t item_tag(unsigned long long t) {
 // any cell of the word spiked, the word's bit in the step's summary row.
 __device__ __forceinline__ void put_hist(const StepArgs& a, const StepIdx& ix, uint32_t w,
                                          uint32_t bits) {
-  const uint32_t r = a.hist_rows - 1u - ix.hrow;  // rows in decreasing step order
-  __stcg(a.hist + (size_t)r * a.n_words + w, bits);
-  __stcg(a.hist + (size_t)(r + a.hist_rows) * a.n_words + w, bits);
+  __stcg(a.hist + (ix.hoff + w), bits);  // rows in decreasing step order
+  __stcg(a.hist + (ix.hoff2 + w), bits);
   if (bits) atomicOr(a.hsum + (size_t)ix.srow * a.n_swords + (w >> 5), 1u << (w & 31u));
 }
 
@@ -190,7 +194,7 @@ __device__ __forceinline__ bool cell_fire(const StepArgs& a, const SegDev& sd, u
                                           const StepIdx& ix) {
   if (!valid) return false;
   if (sd.kind == kSegInput) return mask ? input_fire(a, a.srcs, sd, local, mask, ix.t) : false;
-  int2* rp = reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i;
+  int2* rp = reinterpret_cast<int2*>(a.ring) + (ix.roff + i);
   const int2 acc = __ldcg(rp);
   if (acc.x | acc.y) __stcg(rp, make_int2(0, 0));
   return lif_step(lif_k(sd), a.substeps, st, acc);
@@ -260,7 +264,7 @@ __device__ __forceinline__ WordIn load_word(const StepArgs& a, uint32_t w, const
   const uint32_t i = (w << 5) + (threadIdx.x & 31u);
   WordIn in;
   in.seg = __ldg(a.seg_of_word + w);
-  in.acc = __ldcg(reinterpret_cast<const int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i);
+  in.acc = __ldcg(reinterpret_cast<const int2*>(a.ring) + (ix.roff + i));
   in.u = a.su[i];
   in.g = a.sg[i];
   return in;
@@ -291,7 +295,7 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
       if (mask) fired = input_fire(a, a.srcs, sd, local, mask, ix.t);
     } else {
       if (in.acc.x | in.acc.y)
-        __stcg(reinterpret_cast<int2*>(a.ring) + (size_t)ix.slot * a.n_pad + i, make_int2(0, 0));
+        __stcg(reinterpret_cast<int2*>(a.ring) + (ix.roff + i), make_int2(0, 0));
       const LifK k = lif_k(sd);
       float4 st = state_in(in.u, in.g, k.Vr);
       fired = lif_step(k, a.substeps, st, in.acc);
@@ -460,6 +464,12 @@ __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw,
   return walked;
 }
 
+__device__ __forceinline__ void ix_rows(const StepArgs& a, StepIdx& ix) {
+  ix.roff = ix.slot * a.n_pad;
+  ix.hoff = (a.hist_rows - 1u - ix.hrow) * a.n_words;
+  ix.hoff2 = ix.hoff + a.hist_rows * a.n_words;
+}
+
 __device__ __forceinline__ StepIdx step_of(const StepArgs& a) {
   const Ctl* ctl = a.ctl;
   StepIdx ix;
@@ -468,7 +478,16 @@ __device__ __forceinline__ StepIdx step_of(const StepArgs& a) {
   ix.hrow = ctl->hist_row;
   ix.srow = (uint32_t)(ix.t % (a.hist_rows + 1ull));
   ix.rel = ctl->t_rel;
+  ix_rows(a, ix);
   return ix;
+}
+
+// The next step's indices (persistent kernels).
+__device__ __forceinline__ void ix_advance(const StepArgs& a, StepIdx& ix) {
+  ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+  ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
+  ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
+  ix_rows(a, ix);
 }
 
 // ---- per-step kernels (CUDA-graph driver) ----------------------------------
@@ -871,9 +890,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     walked += deliver_warp<BF16, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
-    ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
-    ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
-    ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
+    ix_advance(a, ix);
   }
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
@@ -937,9 +954,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     walked += deliver_warp<BF16, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) break;
-    ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
-    ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
-    ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
+    ix_advance(a, ix);
   }
   if (valid && lif) state_out(a, i, st);
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
@@ -1212,9 +1227,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       aborted = true;
       break;
     }
-    ix.slot = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
-    ix.hrow = ix.hrow + 1u == a.hist_rows ? 0u : ix.hrow + 1u;
-    ix.srow = ix.srow == a.hist_rows ? 0u : ix.srow + 1u;
+    ix_advance(a, ix);
   }
   if (valid && lif) state_out(a, i, st);
   // The shards of the last step's spikes (ix has advanced past that step).
