@@ -280,17 +280,21 @@ __device__ __forceinline__ void state_out(const StepArgs& a, uint32_t i, const f
   a.sg[i] = make_float2(st.y, st.z);
 }
 
+// RECENT: the handle may keep per-cell spike registers (plastic projections,
+// per-step drivers only); the persistent kernels never do.
+template <bool RECENT = true>
 __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
                                             const StepIdx& ix) {
   if (in.seg == 0xFFFFu) return;  // padding between segments (warp-uniform)
   const uint32_t lane = threadIdx.x & 31u;
   const SegDev& sd = a.segs[in.seg];
+  const uint4 hd = *reinterpret_cast<const uint4*>(&sd);  // base, count, key_base, kind
   const uint32_t i = (w << 5) + lane;
-  const uint32_t local = i - sd.base;
-  const bool valid = local < sd.count;
+  const uint32_t local = i - hd.x;
+  const bool valid = local < hd.y;
   bool fired = false;
   if (valid) {
-    if (sd.kind == kSegInput) {
+    if (hd.w == kSegInput) {
       const uint32_t mask = __ldg(a.src_mask + i);
       if (mask) fired = input_fire(a, a.srcs, sd, local, mask, ix.t);
     } else {
@@ -303,7 +307,7 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
     }
     // Handles with plastic projections (per-step drivers only): each cell's
     // last 64 steps of spikes, bit j = step t - j, for the pairing windows.
-    if (a.recent) a.recent[i] = (a.recent[i] << 1) | (fired ? 1ull : 0ull);
+    if (RECENT && a.recent) a.recent[i] = (a.recent[i] << 1) | (fired ? 1ull : 0ull);
   }
   uint32_t r0 = 0, r1 = 0, od = 0;
   if (fired) {
@@ -331,7 +335,7 @@ __device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uin
     const uint32_t wn = w + nw;
     WordIn nxt;
     if (wn < a.n_words) nxt = load_word(a, wn, ix);
-    finish_word(a, w, cur, ix);
+    finish_word<false>(a, w, cur, ix);
     if (wn >= a.n_words) break;
     w = wn;
     cur = nxt;
