@@ -248,11 +248,13 @@ def plasticity_leg(peak: float, bench_steps: int = 5, chunk: int = 1000):
     synapses): the Teacher rule with the reference's depressing coefficient
     (-0.01 per pre spike in a 50-step window before a teacher spike,
     SynapticPlasticity.cu:13-18), basket cells standing in for the climbing
-    fibre (config 2 has no inferior olive).  Graph driver (plastic projections
-    are delivered by dense pull).  Realtime factor over `bench_steps` chunks and
-    the STDP kernel's per-launch time and algorithmic bytes (per updated
-    plastic synapse 16 B + W; with this rule only the rows of Purkinje cells
-    whose teacher fired are updated)."""
+    fibre (config 2 has no inferior olive); plastic projections are delivered
+    by dense pull.  Realtime factor over `bench_steps` chunks with the
+    persistent kernel (update, plasticity, deliveries as phases between grid
+    barriers) and with the per-step kernels in a CUDA graph, and the STDP
+    kernel's per-launch time and algorithmic bytes (per updated plastic
+    synapse 16 B + W; with this rule only the rows of Purkinje cells whose
+    teacher fired are updated)."""
     import torch
 
     import scaffold_gb300 as sg
@@ -261,25 +263,35 @@ def plasticity_leg(peak: float, bench_steps: int = 5, chunk: int = 1000):
     names = {p.name: p.index for p in net.projections}
     net.add_plasticity(names["granule_to_purkinje"], sg.STDP_TEACHER,
                        teacher=names["basket_to_purkinje"], window=50, a2_ji=-0.01)
-    sim = sg.Simulation([net], [1], chunk_steps=chunk, exec_mode=sg.EXEC_GRAPH)
-    stream = torch.cuda.Stream()
-    sim.set_stream(stream.cuda_stream)
-    sim.run(chunk)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(bench_steps):
-        sim.enqueue(chunk)
-    e1.record(stream)
-    sim.sync()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+
+    def timed(exec_mode):
+        sim = sg.Simulation([net], [1], chunk_steps=chunk, exec_mode=exec_mode)
+        stream = torch.cuda.Stream()
+        sim.set_stream(stream.cuda_stream)
+        sim.run(chunk)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(bench_steps):
+            sim.enqueue(chunk)
+        e1.record(stream)
+        sim.sync()
+        torch.cuda.synchronize()
+        return sim, e0.elapsed_time(e1)
+
+    sim, ms_g = timed(sg.EXEC_GRAPH)
     mean_us, bytes_pl, nl = sim.profile(200)
+    sim.close()
+    sim, ms = timed(sg.EXEC_PERSISTENT)
+    kern = {1: "k_persistent", 2: "k_persistent_resident", 3: "k_persistent_fused"}.get(
+        sim.info().step_kernel, "graph")
     sim.close()
     gbs = bytes_pl[3] / (mean_us[3] * 1e-6) / 1e9 if mean_us[3] > 0 else 0.0
     return {"workload": "config 2, FP32, Teacher STDP on granule_to_purkinje (1,750,000 synapses)",
             "realtime_factor": bench_steps * chunk * 1e-4 / (ms * 1e-3),
-            "us_per_step": 1000.0 * ms / (bench_steps * chunk),
+            "us_per_step": 1000.0 * ms / (bench_steps * chunk), "exec_kernel": kern,
+            "graph_realtime_factor": bench_steps * chunk * 1e-4 / (ms_g * 1e-3),
+            "graph_us_per_step": 1000.0 * ms_g / (bench_steps * chunk),
             "k_stdp_us": mean_us[3], "k_stdp_bytes": bytes_pl[3], "k_stdp_gbs": gbs,
             "k_stdp_frac": gbs / peak, "k_pull_us": mean_us[2], "k_update_us": mean_us[0],
             "k_deliver_us": mean_us[1]}

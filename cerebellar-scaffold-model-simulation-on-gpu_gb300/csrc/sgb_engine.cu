@@ -423,19 +423,14 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   // A plastic synapse with delay d reads its pre cell's spikes d .. d +
   // window - 1 steps back, a teacher up to max_delay steps back.  Windows that
   // end within 64 steps come from the per-cell spike registers instead.
-  bool any_plastic = false;
   for (const Network& net : s.nets)
     for (const Projection& pr : net.projs) {
       if (!pr.plastic) continue;
-      any_plastic = true;
       int dmax = 1;
       for (uint8_t d : pr.delay) dmax = std::max(dmax, (int)d);
       const int back = dmax + pr.plast.window_steps <= 64 ? 0 : dmax + pr.plast.window_steps;
       s.hist_rows = std::max<uint32_t>(s.hist_rows, (uint32_t)std::max(max_delay + 1, back));
     }
-  if (any_plastic && cfg.exec_mode == SGB_EXEC_PERSISTENT)
-    return set_error(SGB_ERR_UNSUPPORTED,
-                     "plastic projections run with the graph or stream driver, not persistent");
   if ((uint64_t)s.hist_rows * s.n_pad > 0xFFFFFFFFull)
     return set_error(SGB_ERR_UNSUPPORTED, "spike history of %u steps x %u cells exceeds 2^32",
                      s.hist_rows, s.n_pad);

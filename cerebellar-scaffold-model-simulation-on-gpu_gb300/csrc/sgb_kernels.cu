@@ -326,6 +326,7 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
 
 // Words gw, gw + nw, ... with the next word's loads in flight while the
 // current one is computed.
+template <bool RECENT>
 __device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uint32_t nw,
                                              const StepIdx& ix) {
   uint32_t w = gw;
@@ -335,7 +336,7 @@ __device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uin
     const uint32_t wn = w + nw;
     WordIn nxt;
     if (wn < a.n_words) nxt = load_word(a, wn, ix);
-    finish_word<false>(a, w, cur, ix);
+    finish_word<RECENT>(a, w, cur, ix);
     if (wn >= a.n_words) break;
     w = wn;
     cur = nxt;
@@ -739,11 +740,12 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
 // it covers), then updates only the units that can change.  Units are
 // kStdpUnit cells, so the rows of the few posts that do change spread over
 // many warps; the window's spike count is gathered eight rows at a time.
+// The plasticity phase of step ix over warps gw, gw + nw, ... (k_stdp, or a
+// phase of the persistent kernels between the update and the deliveries).
 template <bool BF16>
-__global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
+__device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32_t nw,
+                                          const StepIdx& ix) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t gw = (blockIdx.x * kBlock + threadIdx.x) >> 5, nw = (gridDim.x * kBlock) >> 5;
-  const StepIdx ix = step_of(a);
   const uint32_t* hb = hist_base(a, ix.hrow);
   const uint32_t pad = a.hist_rows * a.n_pad;
   for (uint32_t base = gw; base < a.n_stdp_units; base += 32u * nw) {
@@ -768,6 +770,11 @@ __global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
       stdp_unit<BF16>(a, a.stdp_units[base + j * nw], hb, pad);
     }
   }
+}
+
+template <bool BF16>
+__global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
+  stdp_warp<BF16>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5, (gridDim.x * kBlock) >> 5, step_of(a));
 }
 
 // Plastic values back to their start, v_max (the reference starts at 1, its
@@ -889,9 +896,16 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     // Item counter of step t + 1: its last user was the update of step t - 1.
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
-    update_words(a, gw, nw, ix);
+    if (a.n_plast)
+      update_words<true>(a, gw, nw, ix);
+    else
+      update_words<false>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
+    if (a.n_plast) {  // plastic values of step t before its dense deliveries
+      stdp_warp<BF16>(a, gw, nw, ix);
+      if (!grid_barrier(a, target)) return;
+    }
     walked += deliver_warp<BF16, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
     ix_advance(a, ix);
@@ -952,10 +966,15 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     if (has) {
       const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
+      if (a.recent && valid) a.recent[i] = (a.recent[i] << 1) | (fired ? 1ull : 0ull);
       publish_word(a, w, seg, i, fired, r0, r1, od, ix);
     }
     if (!grid_barrier(a, target)) break;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
+    if (a.n_plast) {  // plastic values of step t before its dense deliveries
+      stdp_warp<BF16>(a, gw, nw, ix);
+      if (!grid_barrier(a, target)) break;
+    }
     walked += deliver_warp<BF16, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) break;
     ix_advance(a, ix);

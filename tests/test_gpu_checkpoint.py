@@ -35,14 +35,15 @@ def test_checkpoint_resume_bit_exact(exec_mode):
     b.close()
 
 
-def test_checkpoint_with_plasticity_and_dense_pull():
+@pytest.mark.parametrize("exec_mode", [sg.EXEC_GRAPH, sg.EXEC_PERSISTENT])
+def test_checkpoint_with_plasticity_and_dense_pull(exec_mode):
     net = sg.scaffold(1, 0.25, 8)
     net.add_plasticity(6, sg.STDP_TEACHER, teacher=8, window=20, a1_j=0.0005, a2_ji=-0.004)
-    a = sg.Simulation([net], [8], chunk_steps=200, raster=True)
+    a = sg.Simulation([net], [8], exec_mode=exec_mode, chunk_steps=200, raster=True)
     a.set_propagation(0, 0, sg.PROP_ELL)
     a.loop_n_steps(400)
     blob = a.save_checkpoint()
-    b = sg.Simulation([net], [8], chunk_steps=200, raster=True)
+    b = sg.Simulation([net], [8], exec_mode=exec_mode, chunk_steps=200, raster=True)
     b.set_propagation(0, 0, sg.PROP_ELL)
     b.load_checkpoint(blob)
     assert np.array_equal(a.plastic_values(0, 6), b.plastic_values(0, 6))

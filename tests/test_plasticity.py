@@ -87,11 +87,12 @@ def _plastic_c1(seed):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
-@pytest.mark.parametrize("exec_mode", [sg.EXEC_GRAPH, sg.EXEC_STREAM])
+@pytest.mark.parametrize("exec_mode", [sg.EXEC_GRAPH, sg.EXEC_STREAM, sg.EXEC_PERSISTENT])
 def test_gpu_plasticity_bit_exact(weight, exec_mode):
     """Hebb on granule->Golgi, Teacher (basket cells as teachers) on
     granule->Purkinje: counts, rasters, cell state and every synapse's value
-    equal the FP32 oracle's."""
+    equal the FP32 oracle's (per-step kernels, or the persistent kernel's
+    plasticity phase between its update and delivery phases)."""
     net = _plastic_c1(11)
     steps = 800
     sim = sg.Simulation([net], [11], weight_type=weight, exec_mode=exec_mode, raster=True,
@@ -116,8 +117,6 @@ def test_gpu_plasticity_bit_exact(weight, exec_mode):
 @pytest.mark.gpu
 def test_gpu_plasticity_limits_and_reset():
     net = _plastic_c1(4)
-    with pytest.raises(sg.SgbError):
-        sg.Simulation([net], [4], exec_mode=sg.EXEC_PERSISTENT)
     sim = sg.Simulation([net], [4])
     with pytest.raises(sg.SgbError):
         sim.set_propagation(0, 2, sg.PROP_CSR)
@@ -129,6 +128,28 @@ def test_gpu_plasticity_limits_and_reset():
     assert (sim.plastic_values(0, 6) == 1).all()
     c2, _ = sim.loop_n_steps(300)
     assert np.array_equal(c1, c2)
+    sim.close()
+
+
+@pytest.mark.gpu
+def test_gpu_plasticity_general_persistent_kernel():
+    """A network with more 32-cell words than the grid has warps runs the
+    general persistent kernel (two grid barriers a step, three with the
+    plasticity phase); plastic values and spikes match the oracle."""
+    net = sg.scaffold(1, 20.0, 21)
+    net.add_plasticity(6, sg.STDP_TEACHER, teacher=8, window=20, a1_j=0.0005, a2_ji=-0.004)
+    sim = sg.Simulation([net], [21], exec_mode=sg.EXEC_PERSISTENT, chunk_steps=120)
+    assert sim.info().step_kernel == 1  # SGB_KERNEL_GENERAL
+    c, _ = sim.loop_n_steps(240)
+    o = oracle_py.Oracle(oracle_py.describe(net), seed=21)
+    ec, _ = o.run(240)
+    assert np.array_equal(c, ec)
+    v, ev = sim.plastic_values(0, 6), o.plastic_values(6)
+    assert np.array_equal(v.view(np.uint32), ev.view(np.uint32))
+    assert (v != 1).any()
+    u, g, ref = sim.state()
+    eu, eg, eref = o.state()
+    assert np.array_equal(u.view(np.uint32), eu.view(np.uint32))
     sim.close()
 
 
