@@ -415,7 +415,8 @@ __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, ui
 // during the launch).  Returns the lane's hits.
 template <bool BF16>
 __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit un,
-                                              const uint32_t* hb, uint32_t slot1) {
+                                              const uint32_t* hb, uint32_t slot1,
+                                              const uint32_t* s_sum) {
   constexpr uint32_t B = 8;
   const uint32_t pad = a.hist_rows * a.n_pad;
   const ProjDev& P = a.projs[un.proj];
@@ -427,9 +428,20 @@ __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit 
 #pragma unroll
     for (uint32_t u = 0; u < B; ++u) e[u] = __ldg(P.ell_syn + ob + 32u * u);  // padded to units
     uint32_t hit = 0;
+    if (s_sum) {
+      // The block's staged summary settles most entries; the history word is
+      // read only for those whose 32-cell word had a spike.
 #pragma unroll
-    for (uint32_t u = 0; u < B; ++u)
-      if (e[u] < pad) hit |= ((__ldcg(hb + (e[u] >> 5)) >> (e[u] & 31u)) & 1u) << u;
+      for (uint32_t u = 0; u < B; ++u) {
+        const uint32_t sw = s_sum[e[u] >> 10];
+        if (__funnelshift_r(sw, sw, e[u] >> 5) & 1u)
+          hit |= ((__ldcg(hb + (e[u] >> 5)) >> (e[u] & 31u)) & 1u) << u;
+      }
+    } else {
+#pragma unroll
+      for (uint32_t u = 0; u < B; ++u)
+        if (e[u] < pad) hit |= ((__ldcg(hb + (e[u] >> 5)) >> (e[u] & 31u)) & 1u) << u;
+    }
     hits += __popc(hit);
     while (hit) {
       const uint32_t u = __ffs(hit) - 1;
@@ -440,12 +452,35 @@ __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit 
   return hits;
 }
 
+// The spike summary of steps t - d1, d1 = 0 .. ring_slots - 2 (the delay rows
+// a pull of step t reads; a longer history kept for plasticity is not) into
+// shared memory as rows d1 of n_swords words, plus the zero word that
+// padding entries (row hist_rows) test; threads tid, tid + nthreads, ... with
+// four loads issued before their stores.  The caller synchronizes the block.
+__device__ __forceinline__ void stage_summary(const StepArgs& a, const StepIdx& ix, uint32_t* s_sum,
+                                              uint32_t tid, uint32_t nthreads) {
+  const uint32_t R = a.hist_rows + 1u, n = (a.ring_slots - 1u) * a.n_swords;
+  for (uint32_t j0 = tid; j0 < n; j0 += 4u * nthreads) {
+    uint32_t v[4];
+#pragma unroll
+    for (uint32_t k = 0; k < 4u; ++k) {
+      const uint32_t j = j0 + k * nthreads;
+      const uint32_t d1 = j / a.n_swords, w = j - d1 * a.n_swords;
+      v[k] = j < n ? __ldcg(a.hsum + (size_t)((ix.srow + R - d1) % R) * a.n_swords + w) : 0u;
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < 4u; ++k)
+      if (j0 + k * nthreads < n) s_sum[j0 + k * nthreads] = v[k];
+  }
+  if (tid == 0) s_sum[a.hist_rows * a.n_swords] = 0u;
+}
+
 // Delivery phase for one warp: push items gw, gw + nw, ... up to the first
 // slot not written this step (each delivered item is cleared), then the dense
 // pull units.  Returns the synapses walked by the push items.
 template <bool BF16, bool PULL>
 __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw, uint32_t nw,
-                                                 const StepIdx& ix) {
+                                                 const StepIdx& ix, const uint32_t* s_sum = nullptr) {
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t walked = 0;
   if (a.any_push) {
@@ -462,7 +497,8 @@ __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw,
     const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     uint32_t hits = 0;
     const uint32_t* hb = hist_base(a, ix.hrow);
-    for (uint32_t u = gw; u < a.n_pull_units; u += nw) hits += pull_unit<BF16>(a, a.pull_units[u], hb, slot1);
+    for (uint32_t u = gw; u < a.n_pull_units; u += nw)
+      hits += pull_unit<BF16>(a, a.pull_units[u], hb, slot1, s_sum);
     hits = __reduce_add_sync(kFull, hits);
     if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
   }
@@ -571,23 +607,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
     for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
   }
   if (SUM) {
-    // Only the rows of delays 1 .. ring_slots - 1 are looked up (a longer
-    // history kept for plasticity is not); four words per thread per round
-    // with the loads issued before the stores.
-    const uint32_t R = a.hist_rows + 1u, n = (a.ring_slots - 1u) * a.n_swords;
-    for (uint32_t j0 = threadIdx.x; j0 < n; j0 += 4u * kPullBlock) {
-      uint32_t v[4];
-#pragma unroll
-      for (uint32_t k = 0; k < 4u; ++k) {
-        const uint32_t j = j0 + k * kPullBlock;
-        const uint32_t d1 = j / a.n_swords, w = j - d1 * a.n_swords;
-        v[k] = j < n ? __ldg(a.hsum + (size_t)((ix.srow + R - d1) % R) * a.n_swords + w) : 0u;
-      }
-#pragma unroll
-      for (uint32_t k = 0; k < 4u; ++k)
-        if (j0 + k * kPullBlock < n) s_sum[j0 + k * kPullBlock] = v[k];  // row d1 = step t - d1
-    }
-    if (threadIdx.x == 0) s_sum[a.hist_rows * a.n_swords] = 0u;  // padding's word
+    stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
     __syncthreads();
   }
   const uint32_t* hb = hist_base(a, ix.hrow);
@@ -881,6 +901,7 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
 
 template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
+  extern __shared__ uint32_t s_sum[];  // staged spike summary (dense pulls), when it fits
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -906,7 +927,13 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
       stdp_warp<BF16>(a, gw, nw, ix);
       if (!grid_barrier(a, target)) return;
     }
-    walked += deliver_warp<BF16, true>(a, gw, nw, ix);
+    const uint32_t* sum = nullptr;
+    if (a.n_pull_units && a.pull_sum) {
+      stage_summary(a, ix, s_sum, threadIdx.x, kPersistBlock);
+      __syncthreads();
+      sum = s_sum;
+    }
+    walked += deliver_warp<BF16, true>(a, gw, nw, ix, sum);
     if (!grid_barrier(a, target)) return;
     ix_advance(a, ix);
   }
@@ -926,6 +953,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
 template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepArgs a,
                                                                           uint32_t n_steps) {
+  extern __shared__ uint32_t s_sum[];  // staged spike summary (dense pulls), when it fits
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -975,7 +1003,13 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
       stdp_warp<BF16>(a, gw, nw, ix);
       if (!grid_barrier(a, target)) break;
     }
-    walked += deliver_warp<BF16, true>(a, gw, nw, ix);
+    const uint32_t* sum = nullptr;
+    if (a.n_pull_units && a.pull_sum) {
+      stage_summary(a, ix, s_sum, threadIdx.x, kPersistBlock);
+      __syncthreads();
+      sum = s_sum;
+    }
+    walked += deliver_warp<BF16, true>(a, gw, nw, ix, sum);
     if (!grid_barrier(a, target)) break;
     ix_advance(a, ix);
   }
@@ -1378,7 +1412,13 @@ cudaError_t pull_setup() {
   if ((e = cudaFuncSetAttribute(k_pull<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
-  return cudaFuncSetAttribute(k_pull<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  if ((e = cudaFuncSetAttribute(k_pull<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  // The persistent kernels stage the same summary rows before their deliveries.
+  if ((e = cudaFuncSetAttribute(k_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent_resident<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)))
+    return e;
+  return cudaFuncSetAttribute(k_persistent_resident<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
 }
 
 int pull_blocks_per_sm(const StepArgs& a) {
@@ -1428,8 +1468,8 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                                         : (const void*)k_persistent_resident<false>)
                               : (a.bf16 ? (const void*)k_persistent<true>
                                         : (const void*)k_persistent<false>);
-  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params,
-                                     fused ? a.row_smem : 0, s);
+  const size_t smem = fused ? a.row_smem : (a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0;
+  return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, smem, s);
 }
 
 uint32_t fused_row_smem_max() {
