@@ -264,7 +264,8 @@ int sgb_net_population_info(const sgb_net* net, int32_t pop, sgb_population_info
 int sgb_net_projection_info(const sgb_net* net, int32_t proj, sgb_projection_info* info);
 /* Makes projection `proj` plastic (replaces the reference's Init_Plasticity,
  * SynapticPlasticity.cu:20-34).  A plastic projection is delivered by dense
- * pull (its weights change every step) and needs the graph or stream driver. */
+ * pull (its weights change every step), after the step's plasticity, with any
+ * driver (persistent: resident or general kernel); autotuning is refused. */
 int sgb_net_add_plasticity(sgb_net* net, int32_t proj, const sgb_plasticity_params* params);
 /* *plastic = 1 and the parameters when projection `proj` is plastic, else 0. */
 int sgb_net_plasticity_info(const sgb_net* net, int32_t proj, int32_t* plastic,
