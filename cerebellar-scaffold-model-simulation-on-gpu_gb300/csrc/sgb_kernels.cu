@@ -265,8 +265,10 @@ __device__ __forceinline__ WordIn load_word(const StepArgs& a, uint32_t w, const
   WordIn in;
   in.seg = __ldg(a.seg_of_word + w);
   in.acc = __ldcg(reinterpret_cast<const int2*>(a.ring) + (ix.roff + i));
-  in.u = a.su[i];
-  in.g = a.sg[i];
+  // State streams through L2 only: no L1 allocation for the largest stream,
+  // which would evict the segment descriptors every word reads.
+  in.u = __ldcg(a.su + i);
+  in.g = __ldcg(a.sg + i);
   return in;
 }
 
@@ -276,8 +278,8 @@ __device__ __forceinline__ float4 state_in(float u, float2 g, float vr) {
   return make_float4(ref ? vr : u, g.x, g.y, __int_as_float(ref));
 }
 __device__ __forceinline__ void state_out(const StepArgs& a, uint32_t i, const float4& st) {
-  a.su[i] = pack_u(st.x, __float_as_int(st.w));
-  a.sg[i] = make_float2(st.y, st.z);
+  __stcg(a.su + i, pack_u(st.x, __float_as_int(st.w)));
+  __stcg(a.sg + i, make_float2(st.y, st.z));
 }
 
 // RECENT: the handle may keep per-cell spike registers (plastic projections,
