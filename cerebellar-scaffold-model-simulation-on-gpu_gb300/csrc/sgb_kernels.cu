@@ -1036,6 +1036,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
 // order, each row whole or not at all; rows past the capacity stay in global
 // memory), so a step's pushes read no global memory.
 constexpr uint32_t kBlockItems = 2048;  // push items per block and step (16 KiB)
+// Own rows are cut into items of kFusedChunk synapses (2 per lane): a block
+// usually pushes one or two spikes' rows a step, and smaller items spread
+// their scattered reductions over more of its warps.
+constexpr uint32_t kFusedChunk = 64;
 
 // An item of the fused kernel: (first synapse, length << 23 | flags); flag 1:
 // the synapses are in the block's shared-memory rows, flag 2: a shard of the
@@ -1210,7 +1214,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         const uint32_t n = __popc(ballot);
         const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
         const uint32_t ev = __reduce_add_sync(kFull, fired ? s_od[threadIdx.x] : 0u);
-        nit = fired ? ((rl & 0x7FFFFFFFu) + kPushChunk - 1) / kPushChunk : 0u;
+        nit = fired ? ((rl & 0x7FFFFFFFu) + kFusedChunk - 1) / kFusedChunk : 0u;
         uint32_t incl = nit;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1227,8 +1231,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         }
         off = __shfl_sync(kFull, off, 0) + incl - nit;
         for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
-          const uint32_t q = k * kPushChunk;
-          s_items[off + k] = make_uint2(qb + q, (min(kPushChunk, (rl & 0x7FFFFFFFu) - q) << 23) |
+          const uint32_t q = k * kFusedChunk;
+          s_items[off + k] = make_uint2(qb + q, (min(kFusedChunk, (rl & 0x7FFFFFFFu) - q) << 23) |
                                                     (rl >> 31));
         }
         if (a.raster_cap) {
@@ -1242,12 +1246,18 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         }
       }
     }
-    bool sh_spill = false;
+    // A spiking shard becomes kFusedChunk-synapse items; those past the
+    // list's capacity (from item sh_from on) its thread's warp pushes below.
+    uint32_t sh_from = kNoRow;
     if (sh_ck) {
       const uint4 h = s_sh[threadIdx.x];
       if ((sh_w >> (h.x & 31u)) & 1u) {
-        const uint32_t o = atomicAdd(&s_n[par], 1u);
-        if (o < kBlockItems) s_items[o] = make_uint2(h.y, h.z); else sh_spill = true;
+        const uint32_t len = h.z >> 23, ni = (len + kFusedChunk - 1) / kFusedChunk;
+        const uint32_t o = atomicAdd(&s_n[par], ni);
+        for (uint32_t k = 0; k < ni && o + k < kBlockItems; ++k)
+          s_items[o + k] = make_uint2(h.y + k * kFusedChunk,
+                                      (min(kFusedChunk, len - k * kFusedChunk) << 23) | (h.z & 3u));
+        if (o + ni > kBlockItems) sh_from = o < kBlockItems ? kBlockItems - o : 0u;
       }
     }
     __syncthreads();
@@ -1265,18 +1275,22 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       const uint32_t o = __shfl_sync(kFull, off, src), c = __shfl_sync(kFull, nit, src);
       const uint32_t b0 = __shfl_sync(kFull, qb, src), bl = __shfl_sync(kFull, rl, src);
       for (uint32_t k = o < kBlockItems ? kBlockItems - o : 0; k < c; ++k) {
-        const uint32_t q = k * kPushChunk;
-        const uint2 it = make_uint2(b0 + q, (min(kPushChunk, (bl & 0x7FFFFFFFu) - q) << 23) | (bl >> 31));
+        const uint32_t q = k * kFusedChunk;
+        const uint2 it = make_uint2(b0 + q, (min(kFusedChunk, (bl & 0x7FFFFFFFu) - q) << 23) | (bl >> 31));
         walked += push_any<BF16>(a, s_rows, it, ix.slot, prev);
       }
     }
     if (n_sh) {
-      uint32_t sp = __ballot_sync(kFull, sh_spill);
+      uint32_t sp = __ballot_sync(kFull, sh_from != kNoRow);
       while (sp) {
         const int src = __ffs(sp) - 1;
         sp &= sp - 1;
         const uint4 h = s_sh[wib * 32u + src];
-        walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
+        const uint32_t len = h.z >> 23;
+        for (uint32_t q = __shfl_sync(kFull, sh_from, src) * kFusedChunk; q < len; q += kFusedChunk)
+          walked += push_any<BF16>(
+              a, s_rows, make_uint2(h.y + q, (min(kFusedChunk, len - q) << 23) | (h.z & 3u)), ix.slot,
+              prev);
       }
     }
     grid_arrive(a, target);

@@ -15,12 +15,12 @@ import scaffold_gb300 as sg
 pytestmark = pytest.mark.gpu
 
 
-def _oracle(net, seed, steps, bf16=False, substeps=1, rates=None):
+def _oracle(net, seed, steps, bf16=False, substeps=1, rates=None, raster_cap=None):
     o = oracle_py.Oracle(oracle_py.describe(net), seed=seed, bf16=bf16, substeps=substeps,
                          mode=oracle_py.FP32)
     if rates is not None:
         o.set_rates(rates)
-    counts, (ids, offs) = o.run(steps)
+    counts, (ids, offs) = o.run(steps, raster_cap)
     u, g, ref = o.state()
     return counts, ids, offs, u, g, ref, o.events()
 
@@ -272,5 +272,36 @@ def test_config2_fused_shards_bit_exact(chunk):
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 3, steps)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    assert sim.info().delivered == exp[6]
+    sim.close()
+
+
+@pytest.mark.parametrize("delay", [1, 2])
+def test_fused_kernel_item_list_overflow(delay):
+    """Every one of 4,864 input cells fires every step with 5,000 synapses:
+    with delay 1 each block's own push items exceed its shared-memory list
+    (the overflow is pushed by the warps that made it); with delay 2 the rows
+    are sharded until the shard capacity runs out and the shards' items
+    overflow the list too.  Bit-exact against the oracle."""
+    rng = np.random.default_rng(23)
+    net = sg.Network()
+    ch = [(1.0, 0.0, 1.0, 0.5), (1.0, -80.0, 1.0, 10.0)]
+    src = net.set_neuron_params("src", 4864, 0, 0, 0, 0, 0, 0, 0, sg.INPUT)
+    dst = net.set_neuron_params("dst", 2048, 3.0, -70.0, 2.0, 0.0, -70.0, -50.0, 0.2, sg.NORMAL, ch)
+    fan = 5000
+    pre = np.repeat(np.arange(4864, dtype=np.uint32), fan)
+    post = rng.integers(0, 2048, pre.size, dtype=np.uint32)
+    w = rng.uniform(0.0001, 0.0004, pre.size).astype(np.float32)
+    net.add_projection(src, dst, pre, post, w, delay, sg.CH_EXC, sg.PROP_CSR)
+    net.set_input_stim(src, rate_hz=10000.0)  # fires every 0.1-ms step
+    steps = 40
+    sim = sg.Simulation([net], [9], exec_mode=sg.EXEC_PERSISTENT, raster=True, chunk_steps=20)
+    assert sim.info().step_kernel == 3  # SGB_KERNEL_FUSED
+    if delay == 2:
+        assert 0 < sim.info().shard_cells < 4864
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
+    exp = _oracle(net, 9, steps, raster_cap=1 << 20)
+    _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    assert counts[:, 0].sum() == 4864 * steps
     assert sim.info().delivered == exp[6]
     sim.close()
