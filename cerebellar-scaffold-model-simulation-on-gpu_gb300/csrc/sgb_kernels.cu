@@ -309,7 +309,7 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
     }
     // Handles with plastic projections (per-step drivers only): each cell's
     // last 64 steps of spikes, bit j = step t - j, for the pairing windows.
-    if (RECENT && a.recent) a.recent[i] = (a.recent[i] << 1) | (fired ? 1ull : 0ull);
+    if (RECENT && a.recent) a.recent[i] = (__ldcg(a.recent + i) << 1) | (fired ? 1ull : 0ull);
   }
   uint32_t r0 = 0, r1 = 0, od = 0;
   if (fired) {
@@ -408,7 +408,11 @@ template <bool BF16>
 __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, uint32_t o,
                                          uint32_t slot1) {
   const uint32_t post = P.ell_rowmajor ? o / P.ell_K : o % P.post_count;
-  const int v = __float2int_rn(load_weight<BF16>(P.ell_w, o));
+  // A plastic projection's weights change every step (inside a persistent
+  // launch too): read at L2, not through the non-coherent read-only path.
+  const float wv = BF16 ? __uint_as_float((uint32_t)__ldcg((const unsigned short*)P.ell_w + o) << 16)
+                        : __ldcg((const float*)P.ell_w + o);
+  const int v = __float2int_rn(wv);
   atomicAdd(a.ring + (((size_t)slot1 * a.n_pad + P.post_base + post) << 1) + P.channel, v);
 }
 
@@ -666,9 +670,17 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
 // cell is its pre cell's spike-bit offset for step t + 1 - d above the history
 // row of step t, so the spikes of steps t - d - s are at e + (s + 1) n_pad;
 // the post cell's spike of step t is at its own index, a teacher's at the
-// offset precomputed per post cell.  The history is read-only here.
+// offset precomputed per post cell.  COH: inside a persistent launch the
+// history, spike registers and plastic values were written this launch by
+// other SMs, so they are read at L2 (ld.global.cg); a per-step kernel reads
+// data written by earlier launches and may use the read-only path.
+template <bool COH>
+__device__ __forceinline__ uint32_t ld_coh(const uint32_t* p) {
+  return COH ? __ldcg(p) : __ldg(p);
+}
+template <bool COH>
 __device__ __forceinline__ uint32_t hist_bit(const uint32_t* hb, uint32_t off) {
-  return (__ldg(hb + (off >> 5)) >> (off & 31u)) & 1u;
+  return (ld_coh<COH>(hb + (off >> 5)) >> (off & 31u)) & 1u;
 }
 
 // A synapse whose dw is 0 keeps its value and weight bit for bit, so with a0
@@ -678,16 +690,16 @@ __device__ __forceinline__ uint32_t hist_bit(const uint32_t* hb, uint32_t off) {
 // (four per lane, loads issued together), so the rows of the few posts that
 // do change spread over many warps; the window's spike count is gathered
 // eight rows at a time.
-template <bool BF16>
+template <bool BF16, bool COH>
 __device__ __forceinline__ bool stdp_post_spiked(const StepArgs& a, const PlastDev& L,
                                                  const ProjDev& P, const uint32_t* hb,
                                                  uint32_t post) {
   const uint32_t so = L.rule == SGB_STDP_TEACHER ? __ldg(L.teacher + post) : P.post_base + post;
-  return so != 0xFFFFFFFFu && hist_bit(hb, so);
+  return so != 0xFFFFFFFFu && hist_bit<COH>(hb, so);
 }
 
 // Updates the cells of one unit (the whole warp, four cells per lane).
-template <bool BF16>
+template <bool BF16, bool COH>
 __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
                                           const uint32_t* hb, uint32_t pad) {
   constexpr uint32_t B = kStdpUnit / 32;
@@ -707,7 +719,7 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
   for (uint32_t k = 0; k < B; ++k) {
     const uint32_t o = un.o0 + lane + 32u * k;
     sp[k] = e[k] < pad &&
-            stdp_post_spiked<BF16>(a, L, P, hb, P.ell_rowmajor ? o / P.ell_K : o % P.post_count);
+            stdp_post_spiked<BF16, COH>(a, L, P, hb, P.ell_rowmajor ? o / P.ell_K : o % P.post_count);
   }
 #pragma unroll
   for (uint32_t k = 0; k < B; ++k) {
@@ -720,18 +732,18 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
       // The pre cell's spike register: bit d is step t - d, bits d .. d +
       // window - 1 the window (d + window <= 64 for this projection).
       const uint32_t d = e[k] / a.n_pad + 1u, g = e[k] - (d - 1u) * a.n_pad;
-      const unsigned long long r = a.recent[g] >> d;
+      const unsigned long long r = (COH ? __ldcg(a.recent + g) : __ldg(a.recent + g)) >> d;
       s_pre = (r & 1ull) != 0ull;
       if (sp[k] && L.a2_ji != 0.f)
         nwin = __popcll(L.window == 64u ? r : r & ((1ull << L.window) - 1ull));
     } else {
-      s_pre = hist_bit(hb, e[k] + a.n_pad) != 0u;
+      s_pre = hist_bit<COH>(hb, e[k] + a.n_pad) != 0u;
       if (sp[k] && L.a2_ji != 0.f) {
         for (uint32_t j0 = 0; j0 < L.window; j0 += 8u) {
           uint32_t bit[8];
 #pragma unroll
           for (uint32_t j = 0; j < 8u; ++j)
-            bit[j] = j0 + j < L.window ? hist_bit(hb, e[k] + (j0 + j + 1u) * a.n_pad) : 0u;
+            bit[j] = j0 + j < L.window ? hist_bit<COH>(hb, e[k] + (j0 + j + 1u) * a.n_pad) : 0u;
 #pragma unroll
           for (uint32_t j = 0; j < 8u; ++j) nwin += bit[j];
         }
@@ -742,7 +754,7 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
     if (s_pre) dw = __fadd_rn(dw, L.a1_j);
     if (sp[k]) dw = __fadd_rn(dw, L.a1_i);
     for (uint32_t j = 0; j < nwin; ++j) dw = __fadd_rn(dw, L.a2_ji);
-    float v = __fadd_rn(L.val[o], dw);
+    float v = __fadd_rn(__ldcg(L.val + o), dw);
     v = v < 0.f ? 0.f : (v > L.v_max ? L.v_max : v);
     L.val[o] = v;
     const float tw = __fmul_rn(__ldg(L.w0 + o), v);
@@ -764,7 +776,7 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
 // many warps; the window's spike count is gathered eight rows at a time.
 // The plasticity phase of step ix over warps gw, gw + nw, ... (k_stdp, or a
 // phase of the persistent kernels between the update and the deliveries).
-template <bool BF16>
+template <bool BF16, bool COH>
 __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32_t nw,
                                           const StepIdx& ix) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -782,21 +794,22 @@ __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32
       } else {
         const uint32_t end = min(un.o0 + kStdpUnit, P.ell_n);
         for (uint32_t p = un.o0 / P.ell_K; p <= (end - 1u) / P.ell_K; ++p)
-          active |= stdp_post_spiked<BF16>(a, L, P, hb, p);
+          active |= stdp_post_spiked<BF16, COH>(a, L, P, hb, p);
       }
     }
     uint32_t act = __ballot_sync(kFull, active);
     while (act) {
       const uint32_t j = __ffs(act) - 1;
       act &= act - 1;
-      stdp_unit<BF16>(a, a.stdp_units[base + j * nw], hb, pad);
+      stdp_unit<BF16, COH>(a, a.stdp_units[base + j * nw], hb, pad);
     }
   }
 }
 
 template <bool BF16>
 __global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
-  stdp_warp<BF16>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5, (gridDim.x * kBlock) >> 5, step_of(a));
+  stdp_warp<BF16, false>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5, (gridDim.x * kBlock) >> 5,
+                         step_of(a));
 }
 
 // Plastic values back to their start, v_max (the reference starts at 1, its
@@ -926,7 +939,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     if (!grid_barrier(a, target)) return;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     if (a.n_plast) {  // plastic values of step t before its dense deliveries
-      stdp_warp<BF16>(a, gw, nw, ix);
+      stdp_warp<BF16, true>(a, gw, nw, ix);
       if (!grid_barrier(a, target)) return;
     }
     const uint32_t* sum = nullptr;
@@ -996,13 +1009,13 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     if (has) {
       const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
-      if (a.recent && valid) a.recent[i] = (a.recent[i] << 1) | (fired ? 1ull : 0ull);
+      if (a.recent && valid) a.recent[i] = (__ldcg(a.recent + i) << 1) | (fired ? 1ull : 0ull);
       publish_word(a, w, seg, i, fired, r0, r1, od, ix);
     }
     if (!grid_barrier(a, target)) break;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     if (a.n_plast) {  // plastic values of step t before its dense deliveries
-      stdp_warp<BF16>(a, gw, nw, ix);
+      stdp_warp<BF16, true>(a, gw, nw, ix);
       if (!grid_barrier(a, target)) break;
     }
     const uint32_t* sum = nullptr;
