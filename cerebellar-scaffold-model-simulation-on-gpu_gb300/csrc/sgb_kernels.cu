@@ -1071,7 +1071,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   __shared__ uint32_t s_n[2];  // item count of step parity p; the other one is reset
   __shared__ uint32_t s_wsum[kPersistBlock / 32];
   __shared__ uint4 s_sh[kMaxShards];  // {cell, first synapse, length << 23 | flags, global first}
-  __shared__ uint32_t s_shtot;
+  __shared__ uint32_t s_shtot, s_ptot;
   __shared__ uint32_t s_od[kPersistBlock];  // out-degree of each thread's cell
   // Segment descriptors and stimulus sources, read every step, in shared
   // memory (when few enough): a miss in the small L1 that this kernel's
@@ -1163,31 +1163,41 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   const bool warp_stim = __any_sync(kFull, stim);
   if (lane == 0 && !warp_stim) atomicMax(&s_poller, threadIdx.x);
   // Push rows into shared memory: sb = the row's offset there, or kNoRow.
+  // Rows of at least kLongRow synapses are placed first (a spike of such a
+  // cell is the most work to push), then the others, each in word order.
   constexpr uint32_t kNoRow = 0xFFFFFFFFu;
+  constexpr uint32_t kLongRow = 128;
   uint32_t sb = kNoRow;
   const uint32_t len = r1 - r0;
   if (a.row_smem) {
-    uint32_t incl = len;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t v = __shfl_up_sync(kFull, incl, o);
-      if (lane >= (uint32_t)o) incl += v;
-    }
-    if (lane == 31) s_wsum[wib] = incl;
-    __syncthreads();
-    if (wib == 0) {
-      uint32_t x = s_wsum[lane], xi = x;
+    const uint32_t cap = a.row_smem / (uint32_t)sizeof(uint2);
+    uint32_t used = sharded ? s_shtot : 0u;
+    for (uint32_t pass = 0; pass < 2; ++pass) {
+      const uint32_t lp = (len >= kLongRow) == (pass == 0) ? len : 0u;
+      uint32_t incl = lp;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(kFull, xi, o);
-        if (lane >= (uint32_t)o) xi += v;
+        const uint32_t v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
       }
-      s_wsum[lane] = xi - x;
+      __syncthreads();  // s_wsum's previous readers are done
+      if (lane == 31) s_wsum[wib] = incl;
+      __syncthreads();
+      if (wib == 0) {
+        uint32_t x = s_wsum[lane], xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t v = __shfl_up_sync(kFull, xi, o);
+          if (lane >= (uint32_t)o) xi += v;
+        }
+        s_wsum[lane] = xi - x;
+        if (lane == 31) s_ptot = xi;
+      }
+      __syncthreads();
+      const uint32_t base = used + s_wsum[wib] + incl - lp;
+      if (lp && base <= cap && lp <= cap - base) sb = base;
+      used += s_ptot;
     }
-    __syncthreads();
-    const uint32_t base = (sharded ? s_shtot : 0u) + s_wsum[wib] + incl - len;
-    const uint32_t cap = a.row_smem / (uint32_t)sizeof(uint2);
-    if (len && base <= cap && len <= cap - base) sb = base;
     uint32_t todo = __ballot_sync(kFull, sb != kNoRow);
     while (todo) {
       const int src = __ffs(todo) - 1;
