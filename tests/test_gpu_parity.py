@@ -117,17 +117,22 @@ def test_batched_instances_match_standalone():
         col += npop
 
 
-def test_ten_substeps_reference_structure():
+@pytest.mark.parametrize("exec_mode", [sg.EXEC_GRAPH, sg.EXEC_PERSISTENT])
+def test_ten_substeps_reference_structure(exec_mode):
     """1-ms exchange steps of 10 Euler substeps (the reference's STEP_MAX=10)."""
     net = sg.scaffold(1, 0.25, 4)
     steps = 300
-    sim = sg.Simulation([net], [4], substeps=10, raster=True)
+    sim = sg.Simulation([net], [4], substeps=10, raster=True, exec_mode=exec_mode)
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 4, steps, substeps=10)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
 
 
-def test_rates_reset_and_periodic_input():
+@pytest.mark.parametrize("exec_mode", [sg.EXEC_GRAPH, sg.EXEC_PERSISTENT])
+def test_rates_reset_and_periodic_input(exec_mode):
+    """Rate changes between chunks, a periodic source with a repeating window
+    on a third of the cells (two sources each), reset; the persistent form
+    draws each step's stimulus one step ahead."""
     net = sg.Network()
     ch = [(1.0, 0.0, 1.0, 0.5), (1.0, -80.0, 1.0, 10.0)]
     mf = net.set_neuron_params("mf", 300, 0, 0, 0, 0, 0, 0, 0, sg.INPUT)
@@ -137,7 +142,7 @@ def test_rates_reset_and_periodic_input():
     net.set_input_stim(mf, None, rate_hz=5.0)
     net.set_input_stim(mf, np.arange(0, 300, 3), kind=sg.INPUT_PERIODIC, rate_hz=140.0,
                        phase_ms=2.3, win_period_ms=50.0, win_start_ms=10.0, win_end_ms=30.0)
-    sim = sg.Simulation([net], [21], raster=True, chunk_steps=128)
+    sim = sg.Simulation([net], [21], raster=True, chunk_steps=128, exec_mode=exec_mode)
     o = oracle_py.Oracle(oracle_py.describe(net), seed=21)
     for rates in ([5.0, 140.0], [40.0, 90.0], [0.0, 200.0]):
         sim.set_input_freq(0, rates)
@@ -152,7 +157,7 @@ def test_rates_reset_and_periodic_input():
     sim.reset([21])
     sim.set_input_freq(0, [5.0, 140.0])
     c1, _ = sim.loop_n_steps(500)
-    fresh = sg.Simulation([net], [21], chunk_steps=128)
+    fresh = sg.Simulation([net], [21], chunk_steps=128, exec_mode=exec_mode)
     c2, _ = fresh.loop_n_steps(500)
     assert np.array_equal(c1, c2)
     assert sim.info().step == 500
