@@ -155,7 +155,9 @@ struct StepArgs {
   float2* sg;                     // conductances of channels 0 and 1
   int* ring;                      // int2 per cell per slot, viewed as int[2]
   uint32_t* hist;                 // [2H][n_words]: rows H-1-(t mod H) and 2H-1-(t mod H) hold step t
-  unsigned long long* recent;     // [n_pad] last 64 steps of spikes per cell (plasticity), or NULL
+  unsigned long long* recent;     // [2][n_pad] per-cell spike registers (plasticity), or NULL:
+                                  // the update of step t writes buffer t & 1 (bit j = step
+                                  // t - j) from buffer (t - 1) & 1
   uint32_t* hsum;                 // [H + 1][n_swords]: bit w of row t mod (H + 1) = word w
                                   // of step t had a spike
   uint2* items;                   // [2][item_cap] push work ranges
@@ -169,6 +171,7 @@ struct StepArgs {
   uint32_t ring_slots, hist_rows;
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
+  uint32_t stdp_early;            // every plastic rule reads only earlier steps' spikes (Teacher)
   uint32_t bar_extra;             // tests only: barrier arrivals that never come
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
   uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory

@@ -666,7 +666,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     }
     bytes = align_up(bytes + std::max<size_t>(units.size(), 1) * sizeof(PullUnit), 256);
     s.off_recent = bytes;
-    bytes = align_up(bytes + (size_t)s.n_pad * 8, 256);
+    bytes = align_up(bytes + (size_t)s.n_pad * 16, 256);  // two buffers
     std::vector<size_t> off_w0(s.plast.size()), off_t(s.plast.size());
     for (size_t i = 0; i < s.plast.size(); ++i) {
       PlastHost& ph = s.plast[i];
@@ -731,6 +731,9 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     a.plast = (const PlastDev*)pb;
     a.recent = (unsigned long long*)(pb + s.off_recent);
     a.n_plast = (uint32_t)pd.size();
+    a.stdp_early = 1u;  // the Teacher rule reads its teacher's and pre cells' earlier spikes
+    for (const PlastDev& d : pd)
+      if (d.rule != SGB_STDP_TEACHER) a.stdp_early = 0u;
     a.stdp_units = (const PullUnit*)(pb + off_units);
     a.n_stdp_units = (uint32_t)units.size();
   }
@@ -796,7 +799,7 @@ int sim_reset(Sim& s, const uint64_t* seeds) {
   SGB_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(Ctl), s.stream));
   if (a.n_plast) {
     SGB_CUDA(launch_plast_reset(a, s.deliver_blocks, s.stream));
-    SGB_CUDA(cudaMemsetAsync(a.recent, 0, (size_t)s.n_pad * 8, s.stream));
+    SGB_CUDA(cudaMemsetAsync(a.recent, 0, (size_t)s.n_pad * 16, s.stream));
   }
   SGB_CUDA(cudaMemsetAsync(a.items, 0, (size_t)2 * a.item_cap * sizeof(uint2), s.stream));
   SGB_CUDA(cudaMemsetAsync(a.totals, 0, s.segs.size() * sizeof(double), s.stream));
@@ -1393,7 +1396,7 @@ std::vector<CkptPart> ckpt_parts(const Sim& s) {
                              {a.ctl, sizeof(Ctl)},
                              {a.totals, s.segs.size() * sizeof(double)}};
   const size_t wsz = s.bf16 ? 2 : 4;
-  if (!s.plast.empty()) v.push_back({a.recent, (size_t)s.n_pad * 8});
+  if (!s.plast.empty()) v.push_back({a.recent, (size_t)s.n_pad * 16});
   for (const PlastHost& ph : s.plast) {
     v.push_back({(char*)s.d_plast + ph.off_val, ph.cells * 4});
     v.push_back({const_cast<void*>(s.projs[ph.k].ell_w), ph.cells * wsz});

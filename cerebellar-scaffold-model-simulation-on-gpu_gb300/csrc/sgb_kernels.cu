@@ -309,7 +309,9 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
     }
     // Handles with plastic projections (per-step drivers only): each cell's
     // last 64 steps of spikes, bit j = step t - j, for the pairing windows.
-    if (RECENT && a.recent) a.recent[i] = (__ldcg(a.recent + i) << 1) | (fired ? 1ull : 0ull);
+    if (RECENT && a.recent)
+      a.recent[(ix.t & 1ull) * a.n_pad + i] =
+          (__ldcg(a.recent + ((ix.t + 1ull) & 1ull) * a.n_pad + i) << 1) | (fired ? 1ull : 0ull);
   }
   uint32_t r0 = 0, r1 = 0, od = 0;
   if (fired) {
@@ -699,9 +701,12 @@ __device__ __forceinline__ bool stdp_post_spiked(const StepArgs& a, const PlastD
 }
 
 // Updates the cells of one unit (the whole warp, four cells per lane).
-template <bool BF16, bool COH>
+// EARLY: run during the update of step t (a rule that reads only earlier
+// steps' spikes), so the spike registers are read from the buffer of step
+// t - 1, one bit lower.
+template <bool BF16, bool COH, bool EARLY>
 __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
-                                          const uint32_t* hb, uint32_t pad) {
+                                          const uint32_t* hb, uint32_t pad, unsigned long long t) {
   constexpr uint32_t B = kStdpUnit / 32;
   const uint32_t lane = threadIdx.x & 31u;
   const PlastDev& L = a.plast[un.proj];
@@ -732,7 +737,8 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
       // The pre cell's spike register: bit d is step t - d, bits d .. d +
       // window - 1 the window (d + window <= 64 for this projection).
       const uint32_t d = e[k] / a.n_pad + 1u, g = e[k] - (d - 1u) * a.n_pad;
-      const unsigned long long r = (COH ? __ldcg(a.recent + g) : __ldg(a.recent + g)) >> d;
+      const unsigned long long* rb = a.recent + ((EARLY ? t + 1ull : t) & 1ull) * a.n_pad + g;
+      const unsigned long long r = (COH ? __ldcg(rb) : __ldg(rb)) >> (EARLY ? d - 1u : d);
       s_pre = (r & 1ull) != 0ull;
       if (sp[k] && L.a2_ji != 0.f)
         nwin = __popcll(L.window == 64u ? r : r & ((1ull << L.window) - 1ull));
@@ -776,7 +782,7 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
 // many warps; the window's spike count is gathered eight rows at a time.
 // The plasticity phase of step ix over warps gw, gw + nw, ... (k_stdp, or a
 // phase of the persistent kernels between the update and the deliveries).
-template <bool BF16, bool COH>
+template <bool BF16, bool COH, bool EARLY>
 __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32_t nw,
                                           const StepIdx& ix) {
   const uint32_t lane = threadIdx.x & 31u;
@@ -801,15 +807,15 @@ __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32
     while (act) {
       const uint32_t j = __ffs(act) - 1;
       act &= act - 1;
-      stdp_unit<BF16, COH>(a, a.stdp_units[base + j * nw], hb, pad);
+      stdp_unit<BF16, COH, EARLY>(a, a.stdp_units[base + j * nw], hb, pad, ix.t);
     }
   }
 }
 
 template <bool BF16>
 __global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
-  stdp_warp<BF16, false>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5, (gridDim.x * kBlock) >> 5,
-                         step_of(a));
+  stdp_warp<BF16, false, false>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5,
+                                (gridDim.x * kBlock) >> 5, step_of(a));
 }
 
 // Plastic values back to their start, v_max (the reference starts at 1, its
@@ -936,10 +942,13 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
       update_words<true>(a, gw, nw, ix);
     else
       update_words<false>(a, gw, nw, ix);
+    // Plastic values of step t before its dense deliveries: with rules that
+    // read only earlier steps' spikes, in the update phase itself.
+    if (a.n_plast && a.stdp_early) stdp_warp<BF16, true, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) return;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
-    if (a.n_plast) {  // plastic values of step t before its dense deliveries
-      stdp_warp<BF16, true>(a, gw, nw, ix);
+    if (a.n_plast && !a.stdp_early) {
+      stdp_warp<BF16, true, false>(a, gw, nw, ix);
       if (!grid_barrier(a, target)) return;
     }
     const uint32_t* sum = nullptr;
@@ -1009,13 +1018,18 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     if (has) {
       const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
-      if (a.recent && valid) a.recent[i] = (__ldcg(a.recent + i) << 1) | (fired ? 1ull : 0ull);
+      if (a.recent && valid)
+        a.recent[(ix.t & 1ull) * a.n_pad + i] =
+            (__ldcg(a.recent + ((ix.t + 1ull) & 1ull) * a.n_pad + i) << 1) | (fired ? 1ull : 0ull);
       publish_word(a, w, seg, i, fired, r0, r1, od, ix);
     }
+    // Plastic values of step t before its dense deliveries: with rules that
+    // read only earlier steps' spikes, in the update phase itself.
+    if (a.n_plast && a.stdp_early) stdp_warp<BF16, true, true>(a, gw, nw, ix);
     if (!grid_barrier(a, target)) break;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
-    if (a.n_plast) {  // plastic values of step t before its dense deliveries
-      stdp_warp<BF16, true>(a, gw, nw, ix);
+    if (a.n_plast && !a.stdp_early) {
+      stdp_warp<BF16, true, false>(a, gw, nw, ix);
       if (!grid_barrier(a, target)) break;
     }
     const uint32_t* sum = nullptr;

@@ -173,6 +173,32 @@ def test_gpu_plasticity_window_sources(window):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("window", [40, 64])
+@pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
+def test_gpu_teacher_rule_in_update_phase(window, weight):
+    """The Teacher rule reads only earlier steps' spikes (the teacher's at t -
+    its delay, the pre cells' at t - d - j), so the persistent kernels run it
+    in the update phase itself, reading the previous step's spike registers
+    (window 40) or the history (window 64); bit-exact against the oracle."""
+    net = sg.scaffold(1, 0.25, 13)
+    net.add_plasticity(6, sg.STDP_TEACHER, teacher=8, window=window, a1_j=0.0007, a2_ji=-0.003)
+    sim = sg.Simulation([net], [13], exec_mode=sg.EXEC_PERSISTENT, weight_type=weight,
+                        raster=True, chunk_steps=170)
+    counts, (ids, offs) = sim.loop_n_steps(600, raster=True)
+    o = oracle_py.Oracle(oracle_py.describe(net), seed=13, bf16=weight == sg.WEIGHT_BF16)
+    ec, (eids, eoffs) = o.run(600)
+    assert np.array_equal(counts, ec) and np.array_equal(ids, eids)
+    v, ev = sim.plastic_values(0, 6), o.plastic_values(6)
+    assert np.array_equal(v.view(np.uint32), ev.view(np.uint32))
+    assert (v != 1).any()
+    u, g, ref = sim.state()
+    eu, eg, eref = o.state()
+    assert np.array_equal(u.view(np.uint32), eu.view(np.uint32))
+    assert np.array_equal(g.view(np.uint32), eg.view(np.uint32))
+    sim.close()
+
+
+@pytest.mark.gpu
 def test_gpu_plasticity_start_value_and_sparse_rule():
     """Values start at v_max; with a0 = a1_j = 0 (the reference's Teacher
     coefficients) only rows of posts whose teacher fired change, and the
