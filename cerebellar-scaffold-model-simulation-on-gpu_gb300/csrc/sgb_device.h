@@ -1,26 +1,34 @@
 // Device-resident descriptors and kernel entry points of the step loop.
 //
 // HBM layout (one simulation handle, all instances concatenated):
-//   cells      padded index space: every (instance, population) segment starts
-//              on a 32-cell boundary, so one warp / one spike-bitmap word
-//              never straddles two segments.
-//   state      float4 per cell {u, g_exc_channel0, g_channel1, refractory
-//              steps left (int bits)}: one 16-byte load and store per update.
+//   cells      padded index space (a multiple of 1,024 cells): every (instance,
+//              population) segment starts on a 32-cell boundary, so one warp /
+//              one spike-bitmap word never straddles two segments.
+//   state      SoA: su (float per cell: the potential, or while refractory the
+//              refractory count as a quiet-NaN payload, the cell sitting at
+//              V_reset) and sg (float2 per cell: conductances of channels 0, 1).
 //   ring       int2 per cell per delay slot: fixed-point conductance
 //              increments {exc, inh} arriving at a future step; D = max
 //              delay + 1 slots.  Integer accumulation makes every sum exact
 //              and independent of the order in which spikes are delivered.
-//   history    spike bitmaps of the last H = max delay steps (1 bit per cell).
-//   items      push work of the current step: for every spiking cell, its
-//              push-table row cut into ranges of at most kPushChunk synapses
-//              (uint2 {first synapse, length << 23 | step tag}); a delivered
-//              item is cleared; double-buffered by step parity.
+//   history    spike bitmap rows (1 bit per cell) of the last H steps, kept
+//              twice in decreasing step order, so step t - d sits d rows above
+//              step t's row; plus a summary bit per 32-cell word and step.
+//   items      push work of the current step (per-step and general persistent
+//              kernels): for every spiking cell, its push-table row cut into
+//              ranges of at most kPushChunk synapses (uint2 {first synapse,
+//              length << 23 | step tag}); a delivered item is cleared;
+//              double-buffered by step parity.  The fused persistent kernel
+//              keeps its items, and its blocks' push rows, in shared memory.
 //   push table one cell-major CSR over every projection in event-driven mode
-//              (all instances): synapse word = padded post index | delay << 27
-//              | accumulator << 31, plus the weight pre-multiplied by its
-//              accumulator's 2^S (exact power-of-two scaling) in FP32 or BF16.
-//   ELL tables per projection, post-major (dense pull): word = population-local
-//              pre index | delay << 28, plus the pre-scaled weight.
+//              (all instances), each row's delay-1 synapses first: synapse
+//              word = padded post index | delay << 27 | accumulator << 31, plus
+//              the weight pre-multiplied by its accumulator's 2^S (exact
+//              power-of-two scaling) in FP32 or BF16.
+//   ELL tables per projection, post-major (dense pull): entry = (delay - 1) *
+//              n_pad + padded pre index, the offset of the pre cell's spike bit
+//              above the history row of the pulling step; plus the pre-scaled
+//              weight.  Padding entries point at an always-zero bit.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

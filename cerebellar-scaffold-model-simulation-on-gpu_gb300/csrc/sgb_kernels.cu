@@ -17,9 +17,14 @@
 //            applied on read as at GPUScaffoldSimulation.cu:735).
 // Two drivers run these phases: per-step kernels (replayed from a CUDA graph;
 // kernel boundaries order the phases) and one persistent cooperative kernel
-// per chunk of steps (a bounded grid barrier orders them).  The ring holds
-// int32 fixed-point sums, so push and pull delivery, any launch order and any
-// number of instances give bit-identical conductances.
+// per chunk of steps (a bounded grid barrier orders them).  The persistent
+// kernel comes in three forms: fused (every word resident in one warp, every
+// projection event-driven: update and push share one phase, one barrier a
+// step, push rows and items in shared memory), resident (words resident,
+// some dense pulls: two barriers) and general (more words than warps).  With
+// plastic projections a plasticity phase runs before the deliveries.  The
+// ring holds int32 fixed-point sums, so push and pull delivery, any launch
+// order and any number of instances give bit-identical conductances.
 #include <stdint.h>
 
 #include "sgb_device.h"
