@@ -28,7 +28,7 @@
 //   ELL tables per projection, post-major (dense pull): entry = (delay - 1) *
 //              n_pad + padded pre index, the offset of the pre cell's spike bit
 //              above the history row of the pulling step; plus the pre-scaled
-//              weight.  Padding entries point at an always-zero bit.
+//              weight.  Padding entries (H * n_pad) are skipped by value.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
