@@ -180,6 +180,7 @@ struct StepArgs {
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
   uint32_t stdp_early;            // every plastic rule reads only earlier steps' spikes (Teacher)
+  uint32_t seg_smem;              // general persistent kernel: segment descriptors in shared memory
   uint32_t bar_extra;             // tests only: barrier arrivals that never come
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
   uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory
@@ -219,6 +220,7 @@ cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t pull_setup();
 int pull_blocks_per_sm(const StepArgs& a);
 size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summary rows
+size_t seg_smem_bytes(const StepArgs& a);  // shared memory of the segment descriptors
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
 int persistent_kernel_kind(const StepArgs& a, int blocks);
 

@@ -615,6 +615,9 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.n_swords = n_swords;
   a.hist_rows = s.hist_rows;
   a.pull_sum = pull_sum_bytes(a) <= kPullSumMax ? 1u : 0u;
+  // The general persistent kernel keeps the segment descriptors in shared
+  // memory when they fit beside the staged summary (same attribute limit).
+  a.seg_smem = seg_smem_bytes(a) + (a.pull_sum ? pull_sum_bytes(a) : 0) <= kPullSumMax ? 1u : 0u;
   a.items = (uint2*)(mb + o_items_push);
   a.item_cap = (uint32_t)item_cap;
   a.counts = (uint32_t*)(mb + o_counts);

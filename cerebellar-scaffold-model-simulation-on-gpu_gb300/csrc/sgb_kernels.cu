@@ -289,12 +289,16 @@ __device__ __forceinline__ void state_out(const StepArgs& a, uint32_t i, const f
 
 // RECENT: the handle may keep per-cell spike registers (plastic projections,
 // per-step drivers only); the persistent kernels never do.
-template <bool RECENT = true>
+// SEGSMEM: the segment descriptors are in the general persistent kernel's
+// dynamic shared memory (g_dyn) rather than read from global memory.
+extern __shared__ __align__(16) unsigned char g_dyn[];
+
+template <bool RECENT = true, bool SEGSMEM = false>
 __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
                                             const StepIdx& ix) {
   if (in.seg == 0xFFFFu) return;  // padding between segments (warp-uniform)
   const uint32_t lane = threadIdx.x & 31u;
-  const SegDev& sd = a.segs[in.seg];
+  const SegDev& sd = SEGSMEM ? reinterpret_cast<const SegDev*>(g_dyn)[in.seg] : a.segs[in.seg];
   const uint4 hd = *reinterpret_cast<const uint4*>(&sd);  // base, count, key_base, kind
   const uint32_t i = (w << 5) + lane;
   const uint32_t local = i - hd.x;
@@ -335,7 +339,7 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
 
 // Words gw, gw + nw, ... with the next word's loads in flight while the
 // current one is computed.
-template <bool RECENT>
+template <bool RECENT, bool SEGSMEM>
 __device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uint32_t nw,
                                              const StepIdx& ix) {
   uint32_t w = gw;
@@ -345,7 +349,7 @@ __device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uin
     const uint32_t wn = w + nw;
     WordIn nxt;
     if (wn < a.n_words) nxt = load_word(a, wn, ix);
-    finish_word<RECENT>(a, w, cur, ix);
+    finish_word<RECENT, SEGSMEM>(a, w, cur, ix);
     if (wn >= a.n_words) break;
     w = wn;
     cur = nxt;
@@ -925,9 +929,22 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
   return grid_wait(a, target);
 }
 
+__host__ __device__ __forceinline__ size_t seg_smem_bytes_dev(const StepArgs& a) {
+  return ((size_t)a.n_segs * sizeof(SegDev) + 15) & ~(size_t)15;
+}
+
 template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
-  extern __shared__ uint32_t s_sum[];  // staged spike summary (dense pulls), when it fits
+  // Dynamic shared memory: the segment descriptors every word reads (when
+  // a.seg_smem), then the staged spike summary (dense pulls, when it fits).
+  uint32_t* s_sum = reinterpret_cast<uint32_t*>(g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0));
+  if (a.seg_smem) {
+    const uint4* src = reinterpret_cast<const uint4*>(a.segs);
+    uint4* dst = reinterpret_cast<uint4*>(g_dyn);
+    for (uint32_t j = threadIdx.x; j < a.n_segs * (uint32_t)(sizeof(SegDev) / 16); j += kPersistBlock)
+      dst[j] = src[j];
+    __syncthreads();
+  }
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -944,9 +961,9 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     if (a.n_plast)
-      update_words<true>(a, gw, nw, ix);
+      a.seg_smem ? update_words<true, true>(a, gw, nw, ix) : update_words<true, false>(a, gw, nw, ix);
     else
-      update_words<false>(a, gw, nw, ix);
+      a.seg_smem ? update_words<false, true>(a, gw, nw, ix) : update_words<false, false>(a, gw, nw, ix);
     // Plastic values of step t before its dense deliveries: with rules that
     // read only earlier steps' spikes, in the update phase itself.
     if (a.n_plast && a.stdp_early) stdp_warp<BF16, true, true>(a, gw, nw, ix);
@@ -1430,6 +1447,7 @@ cudaError_t launch_deliver(const StepArgs& a, int blocks, cudaStream_t s) {
 }
 
 size_t pull_sum_bytes(const StepArgs& a) { return ((size_t)a.hist_rows * a.n_swords + 1) * 4; }
+size_t seg_smem_bytes(const StepArgs& a) { return seg_smem_bytes_dev(a); }
 
 static size_t pull_smem_bytes(const StepArgs& a) { return a.pull_sum ? pull_sum_bytes(a) : 0; }
 
@@ -1526,7 +1544,9 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                                         : (const void*)k_persistent_resident<false>)
                               : (a.bf16 ? (const void*)k_persistent<true>
                                         : (const void*)k_persistent<false>);
-  const size_t smem = fused ? a.row_smem : (a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0;
+  const size_t smem = fused ? a.row_smem
+                     : ((resident || !a.seg_smem) ? 0 : seg_smem_bytes(a)) +
+                           ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0);
   return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, smem, s);
 }
 
