@@ -105,6 +105,8 @@ struct SrcDev {
   int64_t win_period, win_start, win_end;  // window in substeps; end <= start: always on
 };
 
+static_assert(sizeof(SrcDev) % 8 == 0, "SrcDev copied in 8-byte units");
+
 struct Ctl {
   unsigned long long step;        // exchange step about to be / being computed
   uint32_t ring_slot;             // step % D

@@ -615,9 +615,6 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.n_swords = n_swords;
   a.hist_rows = s.hist_rows;
   a.pull_sum = pull_sum_bytes(a) <= kPullSumMax ? 1u : 0u;
-  // The general persistent kernel keeps the segment descriptors in shared
-  // memory when they fit beside the staged summary (same attribute limit).
-  a.seg_smem = seg_smem_bytes(a) + (a.pull_sum ? pull_sum_bytes(a) : 0) <= kPullSumMax ? 1u : 0u;
   a.items = (uint2*)(mb + o_items_push);
   a.item_cap = (uint32_t)item_cap;
   a.counts = (uint32_t*)(mb + o_counts);
@@ -628,6 +625,9 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.n_words = s.n_words;
   a.n_segs = (uint32_t)nseg;
   a.n_srcs = (uint32_t)s.srcs.size();
+  // The general persistent kernel keeps the segment descriptors and sources
+  // in shared memory when they fit beside the staged summary (one limit).
+  a.seg_smem = seg_smem_bytes(a) + (a.pull_sum ? pull_sum_bytes(a) : 0) <= kPullSumMax ? 1u : 0u;
   a.n_projs = (uint32_t)s.projs.size();
   a.ring_slots = s.ring_slots;
   a.hist_rows = s.hist_rows;

@@ -289,9 +289,13 @@ __device__ __forceinline__ void state_out(const StepArgs& a, uint32_t i, const f
 
 // RECENT: the handle may keep per-cell spike registers (plastic projections,
 // per-step drivers only); the persistent kernels never do.
-// SEGSMEM: the segment descriptors are in the general persistent kernel's
-// dynamic shared memory (g_dyn) rather than read from global memory.
+// SEGSMEM: the segment descriptors and stimulus sources are in the general
+// persistent kernel's dynamic shared memory (g_dyn: descriptors, then
+// sources) rather than read from global memory.
 extern __shared__ __align__(16) unsigned char g_dyn[];
+__host__ __device__ __forceinline__ size_t seg_table_bytes(uint32_t n_segs) {
+  return ((size_t)n_segs * sizeof(SegDev) + 15) & ~(size_t)15;
+}
 
 template <bool RECENT = true, bool SEGSMEM = false>
 __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
@@ -307,7 +311,9 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
   if (valid) {
     if (hd.w == kSegInput) {
       const uint32_t mask = __ldg(a.src_mask + i);
-      if (mask) fired = input_fire(a, a.srcs, sd, local, mask, ix.t);
+      const SrcDev* srcs =
+          SEGSMEM ? reinterpret_cast<const SrcDev*>(g_dyn + seg_table_bytes(a.n_segs)) : a.srcs;
+      if (mask) fired = input_fire(a, srcs, sd, local, mask, ix.t);
     } else {
       if (in.acc.x | in.acc.y)
         __stcg(reinterpret_cast<int2*>(a.ring) + (ix.roff + i), make_int2(0, 0));
@@ -930,7 +936,7 @@ __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long lo
 }
 
 __host__ __device__ __forceinline__ size_t seg_smem_bytes_dev(const StepArgs& a) {
-  return ((size_t)a.n_segs * sizeof(SegDev) + 15) & ~(size_t)15;
+  return seg_table_bytes(a.n_segs) + (((size_t)a.n_srcs * sizeof(SrcDev) + 15) & ~(size_t)15);
 }
 
 template <bool BF16>
@@ -943,6 +949,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     uint4* dst = reinterpret_cast<uint4*>(g_dyn);
     for (uint32_t j = threadIdx.x; j < a.n_segs * (uint32_t)(sizeof(SegDev) / 16); j += kPersistBlock)
       dst[j] = src[j];
+    const uint2* ss = reinterpret_cast<const uint2*>(a.srcs);
+    uint2* sd = reinterpret_cast<uint2*>(g_dyn + seg_table_bytes(a.n_segs));
+    for (uint32_t j = threadIdx.x; j < a.n_srcs * (uint32_t)(sizeof(SrcDev) / 8); j += kPersistBlock)
+      sd[j] = ss[j];
     __syncthreads();
   }
   Ctl* ctl = a.ctl;
