@@ -1009,7 +1009,21 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
 template <bool BF16>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepArgs a,
                                                                           uint32_t n_steps) {
-  extern __shared__ uint32_t s_sum[];  // staged spike summary (dense pulls), when it fits
+  // Dynamic shared memory as in the general kernel: segment descriptors and
+  // sources (when a.seg_smem), then the staged spike summary.
+  uint32_t* s_sum = reinterpret_cast<uint32_t*>(g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0));
+  if (a.seg_smem) {
+    const uint4* src = reinterpret_cast<const uint4*>(a.segs);
+    uint4* dst = reinterpret_cast<uint4*>(g_dyn);
+    for (uint32_t j = threadIdx.x; j < a.n_segs * (uint32_t)(sizeof(SegDev) / 16); j += kPersistBlock)
+      dst[j] = src[j];
+    const uint2* ss = reinterpret_cast<const uint2*>(a.srcs);
+    uint2* sd = reinterpret_cast<uint2*>(g_dyn + seg_table_bytes(a.n_segs));
+    for (uint32_t j = threadIdx.x; j < a.n_srcs * (uint32_t)(sizeof(SrcDev) / 8); j += kPersistBlock)
+      sd[j] = ss[j];
+    __syncthreads();
+  }
+  const SegDev* segs = a.seg_smem ? reinterpret_cast<const SegDev*>(g_dyn) : a.segs;
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -1049,7 +1063,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     if (has) {
-      const bool fired = cell_fire(a, a.segs[seg], i, local, valid, st, mask, ix);
+      const bool fired = cell_fire(a, segs[seg], i, local, valid, st, mask, ix);
       if (a.recent && valid)
         a.recent[(ix.t & 1ull) * a.n_pad + i] =
             (__ldcg(a.recent + ((ix.t + 1ull) & 1ull) * a.n_pad + i) << 1) | (fired ? 1ull : 0ull);
@@ -1555,7 +1569,7 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                               : (a.bf16 ? (const void*)k_persistent<true>
                                         : (const void*)k_persistent<false>);
   const size_t smem = fused ? a.row_smem
-                     : ((resident || !a.seg_smem) ? 0 : seg_smem_bytes(a)) +
+                     : (a.seg_smem ? seg_smem_bytes(a) : 0) +
                            ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0);
   return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, smem, s);
 }
