@@ -308,26 +308,29 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
   const uint32_t local = i - hd.x;
   const bool valid = local < hd.y;
   bool fired = false;
-  if (valid) {
-    if (hd.w == kSegInput) {
+  if (hd.w == kSegInput) {  // warp-uniform
+    if (valid) {
       const uint32_t mask = __ldg(a.src_mask + i);
       const SrcDev* srcs =
           SEGSMEM ? reinterpret_cast<const SrcDev*>(g_dyn + seg_table_bytes(a.n_segs)) : a.srcs;
       if (mask) fired = input_fire(a, srcs, sd, local, mask, ix.t);
-    } else {
-      if (in.acc.x | in.acc.y)
-        __stcg(reinterpret_cast<int2*>(a.ring) + (ix.roff + i), make_int2(0, 0));
-      const LifK k = lif_k(sd);
-      float4 st = state_in(in.u, in.g, k.Vr);
-      fired = lif_step(k, a.substeps, st, in.acc);
-      state_out(a, i, st);
     }
-    // Handles with plastic projections (per-step drivers only): each cell's
-    // last 64 steps of spikes, bit j = step t - j, for the pairing windows.
-    if (RECENT && a.recent)
-      a.recent[(ix.t & 1ull) * a.n_pad + i] =
-          (__ldcg(a.recent + ((ix.t + 1ull) & 1ull) * a.n_pad + i) << 1) | (fired ? 1ull : 0ull);
+  } else {
+    // Every lane of a LIF word runs the update: a padding lane past the
+    // segment's end integrates its own (never read) padding state and is
+    // masked out of the spikes, so no lane diverges here.
+    if (in.acc.x | in.acc.y)
+      __stcg(reinterpret_cast<int2*>(a.ring) + (ix.roff + i), make_int2(0, 0));
+    const LifK k = lif_k(sd);
+    float4 st = state_in(in.u, in.g, k.Vr);
+    fired = lif_step(k, a.substeps, st, in.acc) && valid;
+    state_out(a, i, st);
   }
+  // Handles with plastic projections: each cell's last 64 steps of spikes,
+  // bit j = step t - j, for the pairing windows.
+  if (RECENT && a.recent && valid)
+    a.recent[(ix.t & 1ull) * a.n_pad + i] =
+        (__ldcg(a.recent + ((ix.t + 1ull) & 1ull) * a.n_pad + i) << 1) | (fired ? 1ull : 0ull);
   uint32_t r0 = 0, r1 = 0, od = 0;
   if (fired) {
     od = __ldg(a.outdeg + i);
