@@ -1073,8 +1073,16 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
       publish_word(a, w, seg, i, fired, r0, r1, od, ix);
     }
     // Plastic values of step t before its dense deliveries: with rules that
-    // read only earlier steps' spikes, in the update phase itself.
-    if (a.n_plast && a.stdp_early) stdp_warp<BF16, true, true>(a, gw, nw, ix);
+    // read only earlier steps' spikes, in the update phase itself, on the
+    // warps without a word (word slots past the last word) when there are
+    // some, so that updates and plasticity run side by side.
+    if (a.n_plast && a.stdp_early) {
+      const uint32_t n_idle = nw > a.n_upd_words ? nw - a.n_upd_words : 0u;
+      if (n_idle == 0u)
+        stdp_warp<BF16, true, true>(a, gw, nw, ix);
+      else if (!has)
+        stdp_warp<BF16, true, true>(a, ws - a.n_upd_words, n_idle, ix);
+    }
     if (!grid_barrier(a, target)) break;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     if (a.n_plast && !a.stdp_early) {
