@@ -439,17 +439,22 @@ __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, ui
 // Persistent kernels: entries straight from global memory, 8 per lane per
 // batch (their 64-register budget), history from L2 (other blocks write it
 // during the launch).  Returns the lane's hits.
+// `part` selects one of the unit's kPullParts ranges of kPullUnit /
+// kPullParts entries (one batch of B per lane): the persistent kernels spread
+// a unit over that many warps, so a pull is one round of loads per warp.
+constexpr uint32_t kPullParts = 4;
 template <bool BF16>
-__device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit un,
+__device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit un, uint32_t part,
                                               const uint32_t* hb, uint32_t slot1,
                                               const uint32_t* s_sum) {
-  constexpr uint32_t B = 8;
+  constexpr uint32_t B = kPullUnit / kPullParts / 32;
   const uint32_t pad = a.hist_rows * a.n_pad;
   const ProjDev& P = a.projs[un.proj];
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t hits = 0;
-#pragma unroll 1
-  for (uint32_t ob = un.o0 + lane; ob < un.o0 + kPullUnit; ob += 32u * B) {
+  const uint32_t o0 = un.o0 + part * (kPullUnit / kPullParts);
+  {
+    const uint32_t ob = o0 + lane;
     uint32_t e[B];
 #pragma unroll
     for (uint32_t u = 0; u < B; ++u) e[u] = __ldg(P.ell_syn + ob + 32u * u);  // padded to units
@@ -523,8 +528,8 @@ __device__ __forceinline__ uint32_t deliver_warp(const StepArgs& a, uint32_t gw,
     const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
     uint32_t hits = 0;
     const uint32_t* hb = hist_base(a, ix.hrow);
-    for (uint32_t u = gw; u < a.n_pull_units; u += nw)
-      hits += pull_unit<BF16>(a, a.pull_units[u], hb, slot1, s_sum);
+    for (uint32_t v = gw; v < a.n_pull_units * kPullParts; v += nw)
+      hits += pull_unit<BF16>(a, a.pull_units[v / kPullParts], v % kPullParts, hb, slot1, s_sum);
     hits = __reduce_add_sync(kFull, hits);
     if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
   }
