@@ -727,9 +727,12 @@ __device__ __forceinline__ bool stdp_post_spiked(const StepArgs& a, const PlastD
 // EARLY: run during the update of step t (a rule that reads only earlier
 // steps' spikes), so the spike registers are read from the buffer of step
 // t - 1, one bit lower.
+// spiked: the screening found the unit inside one post cell's row with its
+// post / teacher spike set, so the entries need not look it up again.
 template <bool BF16, bool COH, bool EARLY>
 __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
-                                          const uint32_t* hb, uint32_t pad, unsigned long long t) {
+                                          const uint32_t* hb, uint32_t pad, unsigned long long t,
+                                          bool spiked = false) {
   constexpr uint32_t B = kStdpUnit / 32;
   const uint32_t lane = threadIdx.x & 31u;
   const PlastDev& L = a.plast[un.proj];
@@ -747,7 +750,8 @@ __device__ __forceinline__ void stdp_unit(const StepArgs& a, const PullUnit un,
   for (uint32_t k = 0; k < B; ++k) {
     const uint32_t o = un.o0 + lane + 32u * k;
     sp[k] = e[k] < pad &&
-            stdp_post_spiked<BF16, COH>(a, L, P, hb, P.ell_rowmajor ? o / P.ell_K : o % P.post_count);
+            (spiked ||
+             stdp_post_spiked<BF16, COH>(a, L, P, hb, P.ell_rowmajor ? o / P.ell_K : o % P.post_count));
   }
 #pragma unroll
   for (uint32_t k = 0; k < B; ++k) {
@@ -813,7 +817,7 @@ __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32
   const uint32_t pad = a.hist_rows * a.n_pad;
   for (uint32_t base = gw; base < a.n_stdp_units; base += 32u * nw) {
     const uint32_t u = base + lane * nw;
-    bool active = false;
+    bool active = false, one = false;  // one: a single post, whose post / teacher spike is set
     if (u < a.n_stdp_units) {
       const PullUnit un = a.stdp_units[u];
       const PlastDev& L = a.plast[un.proj];
@@ -822,15 +826,17 @@ __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32
         active = true;
       } else {
         const uint32_t end = min(un.o0 + kStdpUnit, P.ell_n);
-        for (uint32_t p = un.o0 / P.ell_K; p <= (end - 1u) / P.ell_K; ++p)
-          active |= stdp_post_spiked<BF16, COH>(a, L, P, hb, p);
+        const uint32_t p0 = un.o0 / P.ell_K, p1 = (end - 1u) / P.ell_K;
+        for (uint32_t p = p0; p <= p1; ++p) active |= stdp_post_spiked<BF16, COH>(a, L, P, hb, p);
+        one = active && p0 == p1;
       }
     }
     uint32_t act = __ballot_sync(kFull, active);
+    const uint32_t ones = __ballot_sync(kFull, one);
     while (act) {
       const uint32_t j = __ffs(act) - 1;
       act &= act - 1;
-      stdp_unit<BF16, COH, EARLY>(a, a.stdp_units[base + j * nw], hb, pad, ix.t);
+      stdp_unit<BF16, COH, EARLY>(a, a.stdp_units[base + j * nw], hb, pad, ix.t, (ones >> j) & 1u);
     }
   }
 }
