@@ -217,7 +217,8 @@ int persistent_blocks_per_sm(bool bf16);
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s);
 // STDP of the plastic projections (per-step drivers, between update and pull)
 // and the reset of their values to 1.
-cudaError_t launch_stdp(const StepArgs& a, int blocks, cudaStream_t s);
+// early: beside k_update of the same step (a.stdp_early rules), on another stream.
+cudaError_t launch_stdp(const StepArgs& a, int blocks, cudaStream_t s, bool early = false);
 cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t pull_setup();
 int pull_blocks_per_sm(const StepArgs& a);

@@ -60,6 +60,9 @@ Sim::~Sim() {
   if (d_misc) cudaFree(d_misc);
   if (d_plast) cudaFree(d_plast);
   if (d_shard) cudaFree(d_shard);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (side) cudaStreamDestroy(side);
   if (h_counts) cudaFreeHost(h_counts);
   if (h_raster) cudaFreeHost(h_raster);
   if (h_raster_off) cudaFreeHost(h_raster_off);
@@ -737,6 +740,11 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     a.stdp_early = 1u;  // the Teacher rule reads its teacher's and pre cells' earlier spikes
     for (const PlastDev& d : pd)
       if (d.rule != SGB_STDP_TEACHER) a.stdp_early = 0u;
+    if (a.stdp_early) {
+      SGB_CUDA(cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking));
+      SGB_CUDA(cudaEventCreateWithFlags(&s.ev_fork, cudaEventDisableTiming));
+      SGB_CUDA(cudaEventCreateWithFlags(&s.ev_join, cudaEventDisableTiming));
+    }
     a.stdp_units = (const PullUnit*)(pb + off_units);
     a.n_stdp_units = (uint32_t)units.size();
   }
@@ -826,10 +834,22 @@ static cudaError_t issue_chunk(Sim& s, uint32_t c, cudaStream_t st, int64_t* nla
     L++;
   } else {
     for (uint32_t i = 0; i < c; ++i) {
-      if ((e = launch_update(a, st))) return e;
-      if (a.n_plast) {
-        if ((e = launch_stdp(a, s.deliver_blocks, st))) return e;
+      if (a.n_plast && s.side) {
+        // Early rule: the step's plasticity does not read its update, so the
+        // two run side by side (fork / join; also inside a graph capture).
+        if ((e = cudaEventRecord(s.ev_fork, st))) return e;
+        if ((e = cudaStreamWaitEvent(s.side, s.ev_fork, 0))) return e;
+        if ((e = launch_stdp(a, s.deliver_blocks, s.side, true))) return e;
+        if ((e = launch_update(a, st))) return e;
+        if ((e = cudaEventRecord(s.ev_join, s.side))) return e;
+        if ((e = cudaStreamWaitEvent(st, s.ev_join, 0))) return e;
         L++;
+      } else {
+        if ((e = launch_update(a, st))) return e;
+        if (a.n_plast) {
+          if ((e = launch_stdp(a, s.deliver_blocks, st))) return e;
+          L++;
+        }
       }
       if (a.n_pull_units) {
         if ((e = launch_pull(a, s.pull_blocks, st))) return e;

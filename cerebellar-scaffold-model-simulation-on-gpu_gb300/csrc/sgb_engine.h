@@ -71,6 +71,10 @@ struct Sim {
   void* d_shard = nullptr;    // fused-kernel shards: split points, shard list, per-block offsets
   size_t off_recent = 0;      // per-cell spike registers inside d_plast
   std::vector<PlastHost> plast;
+  // Per-step drivers with early plasticity rules: k_stdp runs on `side`,
+  // forked from and joined back into the step's stream around k_update.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // Persisting L2 window over the cell state (su, sg).
   void* l2_base = nullptr;
   size_t l2_window = 0, l2_setaside = 0, l2_prev_limit = 0;

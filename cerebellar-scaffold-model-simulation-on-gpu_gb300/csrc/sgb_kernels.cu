@@ -841,9 +841,11 @@ __device__ __forceinline__ void stdp_warp(const StepArgs& a, uint32_t gw, uint32
   }
 }
 
-template <bool BF16>
+// EARLY: launched beside k_update of the same step (rules that read only
+// earlier steps' spikes), reading the spike registers of step t - 1.
+template <bool BF16, bool EARLY>
 __global__ void __launch_bounds__(kBlock) k_stdp(StepArgs a) {
-  stdp_warp<BF16, false, false>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5,
+  stdp_warp<BF16, false, EARLY>(a, (blockIdx.x * kBlock + threadIdx.x) >> 5,
                                 (gridDim.x * kBlock) >> 5, step_of(a));
 }
 
@@ -1510,12 +1512,15 @@ cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_stdp(const StepArgs& a, int blocks, cudaStream_t s) {
+cudaError_t launch_stdp(const StepArgs& a, int blocks, cudaStream_t s, bool early) {
   if (!a.n_stdp_units) return cudaSuccess;
-  if (a.bf16)
-    k_stdp<true><<<blocks, kBlock, 0, s>>>(a);
-  else
-    k_stdp<false><<<blocks, kBlock, 0, s>>>(a);
+  if (a.bf16) {
+    if (early) k_stdp<true, true><<<blocks, kBlock, 0, s>>>(a);
+    else k_stdp<true, false><<<blocks, kBlock, 0, s>>>(a);
+  } else {
+    if (early) k_stdp<false, true><<<blocks, kBlock, 0, s>>>(a);
+    else k_stdp<false, false><<<blocks, kBlock, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 

@@ -175,14 +175,17 @@ def test_gpu_plasticity_window_sources(window):
 @pytest.mark.gpu
 @pytest.mark.parametrize("window", [40, 64])
 @pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
-def test_gpu_teacher_rule_in_update_phase(window, weight):
+@pytest.mark.parametrize("exec_mode", [sg.EXEC_PERSISTENT, sg.EXEC_GRAPH, sg.EXEC_STREAM])
+def test_gpu_teacher_rule_in_update_phase(window, weight, exec_mode):
     """The Teacher rule reads only earlier steps' spikes (the teacher's at t -
-    its delay, the pre cells' at t - d - j), so the persistent kernels run it
-    in the update phase itself, reading the previous step's spike registers
-    (window 40) or the history (window 64); bit-exact against the oracle."""
+    its delay, the pre cells' at t - d - j), so it runs beside the step's
+    update: in the persistent kernels' update phase, and with the per-step
+    drivers as k_stdp on a forked stream concurrent with k_update (reading the
+    previous step's spike registers, window 40, or the history, window 64);
+    bit-exact against the oracle."""
     net = sg.scaffold(1, 0.25, 13)
     net.add_plasticity(6, sg.STDP_TEACHER, teacher=8, window=window, a1_j=0.0007, a2_ji=-0.003)
-    sim = sg.Simulation([net], [13], exec_mode=sg.EXEC_PERSISTENT, weight_type=weight,
+    sim = sg.Simulation([net], [13], exec_mode=exec_mode, weight_type=weight,
                         raster=True, chunk_steps=170)
     counts, (ids, offs) = sim.loop_n_steps(600, raster=True)
     o = oracle_py.Oracle(oracle_py.describe(net), seed=13, bf16=weight == sg.WEIGHT_BF16)
