@@ -436,12 +436,12 @@ __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, ui
   atomicAdd(a.ring + (((size_t)slot1 * a.n_pad + P.post_base + post) << 1) + P.channel, v);
 }
 
-// Persistent kernels: entries straight from global memory, 8 per lane per
-// batch (their 64-register budget), history from L2 (other blocks write it
-// during the launch).  Returns the lane's hits.
-// `part` selects one of the unit's kPullParts ranges of kPullUnit /
-// kPullParts entries (one batch of B per lane): the persistent kernels spread
-// a unit over that many warps, so a pull is one round of loads per warp.
+// Persistent kernels: one of a unit's kPullParts ranges of kPullUnit /
+// kPullParts entries (`part`; 8 per lane, loaded at once, within their
+// 64-register budget), so a unit spreads over that many warps and a pull is
+// one round of loads per warp.  Entries straight from global memory, tested
+// against the block's staged summary when there is one, history words from
+// L2 (other blocks write them during the launch).  Returns the lane's hits.
 constexpr uint32_t kPullParts = 4;
 template <bool BF16>
 __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit un, uint32_t part,
