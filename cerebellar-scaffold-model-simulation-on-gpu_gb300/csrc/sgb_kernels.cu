@@ -287,8 +287,10 @@ __device__ __forceinline__ void state_out(const StepArgs& a, uint32_t i, const f
   __stcg(a.sg + i, make_float2(st.y, st.z));
 }
 
-// RECENT: the handle may keep per-cell spike registers (plastic projections,
-// per-step drivers only); the persistent kernels never do.
+// RECENT: the handle may keep per-cell spike registers (plastic
+// projections); the general persistent kernel takes the RECENT = false form
+// when it has none, so the update of a network without plasticity carries
+// no trace of them.
 // SEGSMEM: the segment descriptors and stimulus sources are in the general
 // persistent kernel's dynamic shared memory (g_dyn: descriptors, then
 // sources) rather than read from global memory.
