@@ -205,16 +205,32 @@ __device__ __forceinline__ bool cell_fire(const StepArgs& a, const SegDev& sd, u
   return lif_step(lif_k(sd), a.substeps, st, acc);
 }
 
+template <bool BF16>
+__device__ __forceinline__ uint32_t push_item(const StepArgs& a, uint2 it, uint32_t slot0);
+
+// A block's own push-item list (general persistent kernel with one grid
+// barrier per step): items in shared memory, the step's count.
+constexpr uint32_t kGenItems = 1024;  // items per block and step (8 KiB)
+struct BlockItems {
+  uint2* items;
+  uint32_t* count;
+};
+
 // Spike bookkeeping of one word: bitmap word, per-segment count, event count,
 // raster entries, and the spiking cells' push rows cut into kPushChunk items
-// laid out by a warp-inclusive scan (one atomic reserves the warp's items).
-__device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint32_t seg,
-                                             uint32_t i, bool fired, uint32_t r0, uint32_t r1,
-                                             uint32_t outdeg, const StepIdx& ix) {
+// laid out by a warp-inclusive scan (one atomic reserves the warp's items):
+// in the step's global list, or with LOCAL in the block's list, where the
+// warp itself pushes the items past its capacity (their slots t + d, d >= 1,
+// are read after the step's barrier).  Returns the synapses pushed here.
+template <bool BF16 = false, bool LOCAL = false>
+__device__ __forceinline__ uint32_t publish_word(const StepArgs& a, uint32_t w, uint32_t seg,
+                                                 uint32_t i, bool fired, uint32_t r0, uint32_t r1,
+                                                 uint32_t outdeg, const StepIdx& ix,
+                                                 BlockItems bi = {nullptr, nullptr}) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t ballot = __ballot_sync(kFull, fired);
   if (lane == 0) put_hist(a, ix, w, ballot);
-  if (ballot == 0) return;
+  if (ballot == 0) return 0;
   const uint32_t n = __popc(ballot);
   const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
   const uint32_t ev = __reduce_add_sync(kFull, fired ? outdeg : 0u);
@@ -229,18 +245,38 @@ __device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint
   uint32_t off = 0, roff = 0;
   Ctl* ctl = a.ctl;
   if (lane == 0) {
-    if (tot_items) off = atomicAdd(&ctl->active_count[ix.t & 1], tot_items);
+    if (tot_items) off = LOCAL ? atomicAdd(bi.count, tot_items)
+                               : atomicAdd(&ctl->active_count[ix.t & 1], tot_items);
     atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], n);
     if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
     if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
   }
   off = __shfl_sync(kFull, off, 0) + incl - nit;
-  uint2* items = a.items + (size_t)(ix.t & 1) * a.item_cap;
-  const uint32_t tag = item_tag(ix.t);
-  for (uint32_t k = 0; k < nit; ++k) {
-    const uint32_t q0 = r0 + k * kPushChunk;
-    const uint32_t len = min(kPushChunk, r1 - q0);
-    __stcg(items + off + k, make_uint2(q0, (len << 23) | tag));
+  uint32_t walked = 0;
+  if (LOCAL) {
+    for (uint32_t k = 0; k < nit && off + k < kGenItems; ++k) {
+      const uint32_t q0 = r0 + k * kPushChunk;
+      bi.items[off + k] = make_uint2(q0, min(kPushChunk, r1 - q0) << 23);
+    }
+    uint32_t spill = __ballot_sync(kFull, off + nit > kGenItems);
+    while (spill) {
+      const int src = __ffs(spill) - 1;
+      spill &= spill - 1;
+      const uint32_t o = __shfl_sync(kFull, off, src), c = __shfl_sync(kFull, nit, src);
+      const uint32_t b0 = __shfl_sync(kFull, r0, src), b1 = __shfl_sync(kFull, r1, src);
+      for (uint32_t k = o < kGenItems ? kGenItems - o : 0u; k < c; ++k) {
+        const uint32_t q0 = b0 + k * kPushChunk;
+        walked += push_item<BF16>(a, make_uint2(q0, min(kPushChunk, b1 - q0) << 23), ix.slot);
+      }
+    }
+  } else {
+    uint2* items = a.items + (size_t)(ix.t & 1) * a.item_cap;
+    const uint32_t tag = item_tag(ix.t);
+    for (uint32_t k = 0; k < nit; ++k) {
+      const uint32_t q0 = r0 + k * kPushChunk;
+      const uint32_t len = min(kPushChunk, r1 - q0);
+      __stcg(items + off + k, make_uint2(q0, (len << 23) | tag));
+    }
   }
   if (a.raster_cap) {
     roff = __shfl_sync(kFull, roff, 0);
@@ -251,6 +287,7 @@ __device__ __forceinline__ void publish_word(const StepArgs& a, uint32_t w, uint
         atomicOr(&ctl->error, kErrRasterOverflow);
     }
   }
+  return walked;
 }
 
 // General form, everything from global memory.  The word's state and ring
@@ -299,10 +336,11 @@ __host__ __device__ __forceinline__ size_t seg_table_bytes(uint32_t n_segs) {
   return ((size_t)n_segs * sizeof(SegDev) + 15) & ~(size_t)15;
 }
 
-template <bool RECENT = true, bool SEGSMEM = false>
-__device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
-                                            const StepIdx& ix) {
-  if (in.seg == 0xFFFFu) return;  // padding between segments (warp-uniform)
+template <bool RECENT = true, bool SEGSMEM = false, bool BF16 = false, bool LOCAL = false>
+__device__ __forceinline__ uint32_t finish_word(const StepArgs& a, uint32_t w, const WordIn& in,
+                                                const StepIdx& ix,
+                                                BlockItems bi = {nullptr, nullptr}) {
+  if (in.seg == 0xFFFFu) return 0;  // padding between segments (warp-uniform)
   const uint32_t lane = threadIdx.x & 31u;
   const SegDev& sd = SEGSMEM ? reinterpret_cast<const SegDev*>(g_dyn)[in.seg] : a.segs[in.seg];
   const uint4 hd = *reinterpret_cast<const uint4*>(&sd);  // base, count, key_base, kind
@@ -341,7 +379,7 @@ __device__ __forceinline__ void finish_word(const StepArgs& a, uint32_t w, const
       r1 = __ldg(a.push_row + i + 1);
     }
   }
-  publish_word(a, w, in.seg, i, fired, r0, r1, od, ix);
+  return publish_word<BF16, LOCAL>(a, w, in.seg, i, fired, r0, r1, od, ix, bi);
 }
 
 __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const StepIdx& ix) {
@@ -349,22 +387,23 @@ __device__ __forceinline__ void update_word(const StepArgs& a, uint32_t w, const
 }
 
 // Words gw, gw + nw, ... with the next word's loads in flight while the
-// current one is computed.
-template <bool RECENT, bool SEGSMEM>
-__device__ __forceinline__ void update_words(const StepArgs& a, uint32_t gw, uint32_t nw,
-                                             const StepIdx& ix) {
-  uint32_t w = gw;
-  if (w >= a.n_words) return;
+// current one is computed.  Returns the synapses pushed on the way.
+template <bool RECENT, bool SEGSMEM, bool BF16, bool LOCAL>
+__device__ __forceinline__ uint32_t update_words(const StepArgs& a, uint32_t gw, uint32_t nw,
+                                                 const StepIdx& ix, BlockItems bi) {
+  uint32_t w = gw, walked = 0;
+  if (w >= a.n_words) return 0;
   WordIn cur = load_word(a, w, ix);
   while (true) {
     const uint32_t wn = w + nw;
     WordIn nxt;
     if (wn < a.n_words) nxt = load_word(a, wn, ix);
-    finish_word<RECENT, SEGSMEM>(a, w, cur, ix);
+    walked += finish_word<RECENT, SEGSMEM, BF16, LOCAL>(a, w, cur, ix, bi);
     if (wn >= a.n_words) break;
     w = wn;
     cur = nxt;
   }
+  return walked;
 }
 
 // ---- phase 2: deliveries ------------------------------------------------------
@@ -957,11 +996,61 @@ __host__ __device__ __forceinline__ size_t seg_smem_bytes_dev(const StepArgs& a)
   return seg_table_bytes(a.n_segs) + (((size_t)a.n_srcs * sizeof(SrcDev) + 15) & ~(size_t)15);
 }
 
-template <bool BF16>
+// Raster offsets of a launch with one grid barrier per step: a block may
+// already reserve raster entries of step s while another still reads the
+// count of step s - 1, so the offsets come from the step counts instead (a
+// step's entries are contiguous: its reservations all follow the previous
+// barrier).  After the launch's last barrier every count is final; block 0
+// scans them (all its threads call this; s_wsum holds kPersistBlock / 32).
+__device__ void raster_offsets_from_counts(const StepArgs& a, uint32_t n_steps, uint32_t* s_wsum) {
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint32_t per = (n_steps + kPersistBlock - 1) / kPersistBlock;
+  const uint32_t q0 = min(n_steps, threadIdx.x * per), q1 = min(n_steps, q0 + per);
+  uint32_t tot = 0;
+  for (uint32_t q = q0; q < q1; ++q)
+    for (uint32_t g = 0; g < a.n_segs; ++g) tot += __ldcg(a.counts + (size_t)q * a.n_segs + g);
+  uint32_t incl = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= (uint32_t)o) incl += v;
+  }
+  __syncthreads();  // s_wsum's previous readers are done
+  if (lane == 31) s_wsum[wib] = incl;
+  __syncthreads();
+  if (wib == 0) {
+    const uint32_t x = s_wsum[lane];
+    uint32_t xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(kFull, xi, o);
+      if (lane >= (uint32_t)o) xi += v;
+    }
+    s_wsum[lane] = xi - x;
+  }
+  __syncthreads();
+  uint32_t run = s_wsum[wib] + incl - tot;
+  for (uint32_t q = q0; q < q1; ++q) {
+    for (uint32_t g = 0; g < a.n_segs; ++g) run += __ldcg(a.counts + (size_t)q * a.n_segs + g);
+    a.raster_off[q + 1] = run;
+  }
+}
+
+// General persistent kernel.  ONE (networks without dense pulls or rules that
+// read the step's own spikes): a step's pushes only target ring slots
+// t + 1 .. t + D while its update reads slot t, so each block collects its
+// spiking cells' push items in shared memory during the update, delivers them
+// right after it, and one grid barrier ends the step.  Otherwise the items go
+// to a global list delivered by all warps between two grid barriers.
+template <bool BF16, bool ONE>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
   // Dynamic shared memory: the segment descriptors every word reads (when
   // a.seg_smem), then the staged spike summary (dense pulls, when it fits).
   uint32_t* s_sum = reinterpret_cast<uint32_t*>(g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0));
+  __shared__ uint2 s_items[ONE ? kGenItems : 1];
+  __shared__ uint32_t s_icnt[2];  // item count of step parity p; the other one is reset
+  __shared__ uint32_t s_wsum[kPersistBlock / 32];
+  if (threadIdx.x == 0) s_icnt[0] = s_icnt[1] = 0;
   if (a.seg_smem) {
     const uint4* src = reinterpret_cast<const uint4*>(a.segs);
     uint4* dst = reinterpret_cast<uint4*>(g_dyn);
@@ -971,8 +1060,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     uint2* sd = reinterpret_cast<uint2*>(g_dyn + seg_table_bytes(a.n_segs));
     for (uint32_t j = threadIdx.x; j < a.n_srcs * (uint32_t)(sizeof(SrcDev) / 8); j += kPersistBlock)
       sd[j] = ss[j];
-    __syncthreads();
   }
+  __syncthreads();
   Ctl* ctl = a.ctl;
   StepIdx ix = step_of(a);
   const unsigned long long t0 = ix.t;
@@ -985,16 +1074,31 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
   for (uint32_t s = 0; s < n_steps; ++s) {
     ix.t = t0 + s;
     ix.rel = s;
-    // Item counter of step t + 1: its last user was the update of step t - 1.
+    // Item counter of step t + 1: its last user was the update of step t - 1
+    // (kept zero in ONE launches too, for launches of the other form).
     if (leader) __stcg(&ctl->active_count[(ix.t + 1) & 1], 0u);
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
+    const BlockItems bi{s_items, &s_icnt[s & 1u]};
     if (a.n_plast)
-      a.seg_smem ? update_words<true, true>(a, gw, nw, ix) : update_words<true, false>(a, gw, nw, ix);
+      walked += a.seg_smem ? update_words<true, true, BF16, ONE>(a, gw, nw, ix, bi)
+                           : update_words<true, false, BF16, ONE>(a, gw, nw, ix, bi);
     else
-      a.seg_smem ? update_words<false, true>(a, gw, nw, ix) : update_words<false, false>(a, gw, nw, ix);
+      walked += a.seg_smem ? update_words<false, true, BF16, ONE>(a, gw, nw, ix, bi)
+                           : update_words<false, false, BF16, ONE>(a, gw, nw, ix, bi);
     // Plastic values of step t before its dense deliveries: with rules that
     // read only earlier steps' spikes, in the update phase itself.
     if (a.n_plast && a.stdp_early) stdp_warp<BF16, true, true>(a, gw, nw, ix);
+    if (ONE) {
+      __syncthreads();
+      const uint32_t n_items = min(s_icnt[s & 1u], kGenItems);
+      // The other parity's count was last read before the previous barrier.
+      if (threadIdx.x == 0) s_icnt[(s & 1u) ^ 1u] = 0;
+      for (uint32_t u = threadIdx.x >> 5; u < n_items; u += kPersistBlock / 32)
+        walked += push_item<BF16>(a, s_items[u], ix.slot);
+      if (!grid_barrier(a, target)) return;
+      ix_advance(a, ix);
+      continue;
+    }
     if (!grid_barrier(a, target)) return;
     if (a.raster_cap && leader) a.raster_off[s + 1] = __ldcg(&ctl->raster_count);
     if (a.n_plast && !a.stdp_early) {
@@ -1011,6 +1115,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     if (!grid_barrier(a, target)) return;
     ix_advance(a, ix);
   }
+  if (ONE && a.raster_cap && blockIdx.x == 0) raster_offsets_from_counts(a, n_steps, s_wsum);
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
     ctl->step = t0 + n_steps;
@@ -1428,43 +1533,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
     }
   }
-  // Raster offsets: with one barrier per step a block may already reserve
-  // raster entries of step s while another still reads the count of step
-  // s - 1, so the offsets come from the step counts instead (a step's
-  // entries are contiguous: its reservations all follow the previous
-  // barrier).  After the last barrier every count is final; block 0 scans.
-  if (a.raster_cap && blockIdx.x == 0) {
-    const uint32_t per = (n_steps + kPersistBlock - 1) / kPersistBlock;
-    const uint32_t q0 = min(n_steps, threadIdx.x * per), q1 = min(n_steps, q0 + per);
-    uint32_t tot = 0;
-    for (uint32_t q = q0; q < q1; ++q)
-      for (uint32_t g = 0; g < a.n_segs; ++g) tot += __ldcg(a.counts + (size_t)q * a.n_segs + g);
-    uint32_t incl = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t v = __shfl_up_sync(kFull, incl, o);
-      if (lane >= (uint32_t)o) incl += v;
-    }
-    __syncthreads();  // s_wsum's last readers were in the prologue
-    if (lane == 31) s_wsum[wib] = incl;
-    __syncthreads();
-    if (wib == 0) {
-      const uint32_t x = s_wsum[lane];
-      uint32_t xi = x;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(kFull, xi, o);
-        if (lane >= (uint32_t)o) xi += v;
-      }
-      s_wsum[lane] = xi - x;
-    }
-    __syncthreads();
-    uint32_t run = s_wsum[wib] + incl - tot;
-    for (uint32_t q = q0; q < q1; ++q) {
-      for (uint32_t g = 0; g < a.n_segs; ++g) run += __ldcg(a.counts + (size_t)q * a.n_segs + g);
-      a.raster_off[q + 1] = run;
-    }
-  }
+  if (a.raster_cap && blockIdx.x == 0) raster_offsets_from_counts(a, n_steps, s_wsum);
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
   if (leader) {
@@ -1543,8 +1612,10 @@ cudaError_t pull_setup() {
   if ((e = cudaFuncSetAttribute(k_pull<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   // The persistent kernels stage the same summary rows before their deliveries.
-  if ((e = cudaFuncSetAttribute(k_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
-  if ((e = cudaFuncSetAttribute(k_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent_resident<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)))
     return e;
   return cudaFuncSetAttribute(k_persistent_resident<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -1565,17 +1636,27 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
 int persistent_blocks_per_sm(bool bf16) {
   int n = 0, m = 0;
   int f = 0;
+  int o = 0;
   if (bf16) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<true, true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<true>, kPersistBlock, 0);
   } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<false, true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<false>, kPersistBlock, 0);
   }
   n = n < m ? n : m;
+  n = n < o ? n : o;
   return n < f ? n : f;
+}
+
+// The general kernel's one-barrier form: no dense pulls, no plastic rule
+// that reads the step's own spikes.
+bool general_one_barrier(const StepArgs& a) {
+  return a.n_pull_units == 0 && (a.n_plast == 0 || a.stdp_early);
 }
 
 int persistent_kernel_kind(const StepArgs& a, int blocks) {
@@ -1595,8 +1676,10 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                                         : (const void*)k_persistent_fused<false>)
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
                                         : (const void*)k_persistent_resident<false>)
-                              : (a.bf16 ? (const void*)k_persistent<true>
-                                        : (const void*)k_persistent<false>);
+                   : general_one_barrier(a)
+                       ? (a.bf16 ? (const void*)k_persistent<true, true> : (const void*)k_persistent<false, true>)
+                       : (a.bf16 ? (const void*)k_persistent<true, false>
+                                 : (const void*)k_persistent<false, false>);
   const size_t smem = fused ? a.row_smem
                      : (a.seg_smem ? seg_smem_bytes(a) : 0) +
                            ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0);

@@ -312,6 +312,35 @@ def test_fused_kernel_item_list_overflow(delay):
     sim.close()
 
 
+@pytest.mark.parametrize("delay", [1, 3])
+def test_general_kernel_block_item_overflow(delay):
+    """163,840 input cells (more 32-cell words than the grid has warps: the
+    general persistent kernel, in its one-barrier form since every projection
+    is event-driven) fire every step with 8 synapses each: every block makes
+    more push items a step than its shared-memory list holds, and the warps
+    push the rest themselves.  Bit-exact against the oracle."""
+    rng = np.random.default_rng(29)
+    net = sg.Network()
+    ch = [(1.0, 0.0, 1.0, 0.5), (1.0, -80.0, 1.0, 10.0)]
+    n_src, n_dst, fan = 163840, 4096, 8
+    src = net.set_neuron_params("src", n_src, 0, 0, 0, 0, 0, 0, 0, sg.INPUT)
+    dst = net.set_neuron_params("dst", n_dst, 3.0, -70.0, 2.0, 0.0, -70.0, -50.0, 0.2, sg.NORMAL, ch)
+    pre = np.repeat(np.arange(n_src, dtype=np.uint32), fan)
+    post = rng.integers(0, n_dst, pre.size, dtype=np.uint32)
+    w = rng.uniform(0.0002, 0.0008, pre.size).astype(np.float32)
+    net.add_projection(src, dst, pre, post, w, delay, sg.CH_EXC, sg.PROP_CSR)
+    net.set_input_stim(src, rate_hz=10000.0)  # fires every 0.1-ms step
+    steps = 20
+    sim = sg.Simulation([net], [4], exec_mode=sg.EXEC_PERSISTENT, raster=True, chunk_steps=10)
+    assert sim.info().step_kernel == 1  # SGB_KERNEL_GENERAL
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True, raster_cap=1 << 22)
+    exp = _oracle(net, 4, steps, raster_cap=1 << 22)
+    _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    assert counts[:, 0].sum() == n_src * steps and counts[:, 1].sum() > 0
+    assert sim.info().delivered == exp[6]
+    sim.close()
+
+
 def test_many_segments_fall_back_to_global_descriptors():
     """250 batched instances (1,750 segments): the persistent kernels' copy of
     the segment descriptors no longer fits in shared memory, so the general
