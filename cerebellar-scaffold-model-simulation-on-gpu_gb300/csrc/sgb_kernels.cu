@@ -1068,6 +1068,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t gw = (blockIdx.x * kPersistBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kPersistBlock) >> 5;
+  // One-barrier form: update words are dealt warp-major over the blocks
+  // (slot = warp x blocks + block), so consecutive words -- a stimulated input
+  // segment, say -- spread over all blocks; each row of nw words is still
+  // swept together.
+  const uint32_t uw = ONE ? (threadIdx.x >> 5) * gridDim.x + blockIdx.x : gw;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
   unsigned long long target = 0;
   uint32_t walked = 0;
@@ -1080,11 +1085,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
     const BlockItems bi{s_items, &s_icnt[s & 1u]};
     if (a.n_plast)
-      walked += a.seg_smem ? update_words<true, true, BF16, ONE>(a, gw, nw, ix, bi)
-                           : update_words<true, false, BF16, ONE>(a, gw, nw, ix, bi);
+      walked += a.seg_smem ? update_words<true, true, BF16, ONE>(a, uw, nw, ix, bi)
+                           : update_words<true, false, BF16, ONE>(a, uw, nw, ix, bi);
     else
-      walked += a.seg_smem ? update_words<false, true, BF16, ONE>(a, gw, nw, ix, bi)
-                           : update_words<false, false, BF16, ONE>(a, gw, nw, ix, bi);
+      walked += a.seg_smem ? update_words<false, true, BF16, ONE>(a, uw, nw, ix, bi)
+                           : update_words<false, false, BF16, ONE>(a, uw, nw, ix, bi);
     // Plastic values of step t before its dense deliveries: with rules that
     // read only earlier steps' spikes, in the update phase itself.
     if (a.n_plast && a.stdp_early) stdp_warp<BF16, true, true>(a, gw, nw, ix);
