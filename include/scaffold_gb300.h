@@ -174,7 +174,8 @@ typedef struct sgb_sim_info {
 
 /* Step kernels (sgb_sim_info.step_kernel). */
 #define SGB_KERNEL_GRAPH 0      /* k_update + k_deliver per step, CUDA graph or stream */
-#define SGB_KERNEL_GENERAL 1    /* persistent; one grid barrier per step, two with dense pulls */
+#define SGB_KERNEL_GENERAL 1    /* persistent; one grid barrier per step (two with dense  */
+                                /* pulls or a Hebbian rule)                               */
 #define SGB_KERNEL_RESIDENT 2   /* persistent, state in registers, two barriers        */
 #define SGB_KERNEL_FUSED 3      /* persistent, state in registers, one barrier         */
 
