@@ -21,7 +21,9 @@
 // kernel comes in three forms: fused (every word resident in one warp, every
 // projection event-driven: update and push share one phase, one barrier a
 // step, push rows and items in shared memory), resident (words resident,
-// some dense pulls: two barriers) and general (more words than warps).  With
+// some dense pulls: two barriers) and general (more words than warps; one
+// barrier a step with the pushes in each block's shared memory when every
+// projection is event-driven, else two with a global item list).  With
 // plastic projections a plasticity phase runs before the deliveries.  The
 // ring holds int32 fixed-point sums, so push and pull delivery, any launch
 // order and any number of instances give bit-identical conductances.
