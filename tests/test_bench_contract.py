@@ -1,0 +1,38 @@
+"""bench.py's reference arm on the CPU: one JSON line with the benchmark's keys.
+
+The reference arm times the reference's own CPU implementation of the step
+(its compiled host functions where the sources are present, else their
+bit-exact restatement) on the host cores, so it runs without a GPU; the GPU
+arm's line carries the same metric, unit and config.
+"""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_json_line():
+    out = subprocess.run(
+        [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2",
+         "--warmup", "0", "--ref-sample", "3"],
+        cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [x for x in out.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"].startswith("realtime factor")
+    assert d["unit"] == "x realtime" and d["higher_is_better"] is True
+    assert d["steps"] == 2 and d["warmup"] == 0 and d["n_gpus"] == 1
+    assert d["value"] > 0 and d["ms_per_step"] > 0
+    assert d["config"]["workload"].startswith("config 2")
+    assert d["config"]["steps_per_bench_step"] == 3
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1
+    assert cb["sample"] == "2 x 3 exchange steps"
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
