@@ -24,6 +24,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 FALLBACK_HBM_GBS = 6800.0
 METRIC = "realtime factor (biological s per wall s), 100k-cell scaffold"
+DATA = "synthetic: seeded fixed in-degree connectivity, Philox Poisson mossy input"
 WORKLOADS = {
     "c2": dict(config=2, scale=1.0, instances=1, bf16=False,
                desc="config 2: 92,550-cell scaffold, 2,731,520 synapses, FP32 weights, 1 instance"),
@@ -47,8 +48,6 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--chunk", type=int, default=1000, help="exchange steps per bench step")
-    ap.add_argument("--ref-sample", type=int, default=100,
-                    help="exchange steps per bench step of the reference arm")
     ap.add_argument("--cpu-sample", type=int, default=20000,
                     help="exchange steps of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -164,10 +163,8 @@ def measured_hbm():
 def cpu_baseline(wl: dict, sample_steps: int):
     """Reference CPU path on a bounded sample of the workload, all host threads."""
     import oracle_py
-    import scaffold_gb300 as sg
 
-    net = sg.scaffold(wl["config"], wl["scale"] or 1.0, 1)
-    desc = oracle_py.describe(net)
+    desc = oracle_py.scaffold_desc(wl["config"], wl["scale"] or 1.0, 1)
     threads = os.cpu_count() or 1
     if oracle_py.have_ref_harness(1):
         ref, kind = oracle_py.RefHarness(desc, seed=1, bf16=wl["bf16"]), "reference"
@@ -208,7 +205,7 @@ def config1_leg(steps: int = 10_000):
     torch.cuda.synchronize()
     gpu_rtf = steps * 1e-4 / (e0.elapsed_time(e1) * 1e-3)
     sim.close()
-    desc = oracle_py.describe(net)
+    desc = oracle_py.scaffold_desc(1, 1.0, 1)
     threads = os.cpu_count() or 1
     if oracle_py.have_ref_harness(1):
         ref, kind = oracle_py.RefHarness(desc, seed=1), "reference"
@@ -333,38 +330,65 @@ def ell_roofline(peak: float):
             "l2": "entries 437 MB per launch (not L2-resident); no flush between launches"}
 
 
+def workload_config(wl: dict, cells: int, synapses: int, instances: int, chunk: int,
+                    world: int) -> dict:
+    """The `config` object of both arms' JSON lines: the workload and the
+    measurement protocol, nothing that depends on the implementation."""
+    return {"workload": wl["desc"], "cells": cells, "synapses": synapses,
+            "instances_per_gpu": instances, "dt_ms": 0.1, "steps_per_bench_step": chunk,
+            "bio_s_per_bench_step": chunk * 0.1e-3 * instances,
+            "weights": "bf16" if wl["bf16"] else "fp32",
+            "l2": "GPU arm: L2 flushed (256 MiB write) before every timed bench step; the cell "
+                  "state kept in a persisting L2 window is exempt by design",
+            "parallelism": f"replicas x{world}"}
+
+
+def reference_desc(wl: dict):
+    """Network of the reference arm, drawn by the oracle's generator (no
+    library code): the same synapse arrays as the GPU arm's instance 0."""
+    import oracle_py
+
+    return oracle_py.scaffold_desc(wl["config"], wl["scale"] or 1.0, 1)
+
+
 def run_reference(a):
+    """The reference's CPU loops (host_update_lif_ch / host_spike_propagation,
+    its compiled functions where they are built, else their restatement) on
+    all host cores, over the GPU arm's workload: one bench step = `--chunk`
+    exchange steps of one instance."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import oracle_py
-    import scaffold_gb300 as sg
 
     wl = WORKLOADS[a.workload]
-    net = sg.scaffold(wl["config"], wl["scale"] or 1.0, 1)
-    desc = oracle_py.describe(net)
+    desc = reference_desc(wl)
+    cells, synapses = oracle_py.desc_counts(desc)
     threads = os.cpu_count() or 1
     if oracle_py.have_ref_harness(1):
         ref, kind = oracle_py.RefHarness(desc, seed=1, bf16=wl["bf16"]), "reference"
     else:
         ref, kind = oracle_py.RefPort(desc, seed=1, bf16=wl["bf16"]), "port"
     for _ in range(a.warmup):
-        ref.run(a.ref_sample, threads=threads)
+        ref.run(a.chunk, threads=threads)
     t0 = time.perf_counter()
     for _ in range(a.steps):
-        ref.run(a.ref_sample, threads=threads)
+        ref.run(a.chunk, threads=threads)
     dt = time.perf_counter() - t0
-    bio = a.steps * a.ref_sample * 0.1e-3
+    bio = a.steps * a.chunk * 0.1e-3
     rtf = bio / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": rtf, "unit": "x realtime",
         "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1000.0 * dt / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl["desc"], "steps_per_bench_step": a.ref_sample, "dt_ms": 0.1,
-                   "threads": threads},
+        "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": workload_config(wl, cells, synapses, 1, a.chunk, world),
+        "engine": {"kind": kind, "threads": threads,
+                   "path": "dense per-delay ELL pull + LIF update (host_spike_propagation / "
+                           "host_update_lif_ch), OpenMP over post cells"},
         "cpu_baseline": {"value": rtf, "unit": "x realtime", "cores": threads, "kind": kind,
-                         "sample": f"{a.steps} x {a.ref_sample} exchange steps"},
+                         "sample": f"{a.steps} bench steps of {a.chunk} exchange steps "
+                                   f"(0.1 ms) of instance 0"},
         "e2e": {"value": rtf, "unit": "x realtime", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -520,22 +544,17 @@ def run_gb300(a):
         "metric": METRIC, "value": value, "unit": "x realtime", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded fixed in-degree connectivity, Philox Poisson mossy input",
-        "config": {"workload": wl["desc"], "cells": info.n_neurons, "synapses": info.n_synapses,
-                   "instances_per_gpu": len(nets), "dt_ms": 0.1,
-                   "steps_per_bench_step": a.chunk, "bio_s_per_bench_step": bio_per_step,
-                   "weights": "bf16" if wl["bf16"] else "fp32",
-                   "exec": {sg.EXEC_PERSISTENT: "one persistent cooperative kernel per chunk",
+        "data": DATA,
+        "config": workload_config(wl, info.n_neurons, info.n_synapses, len(nets), a.chunk,
+                                  world),
+        "engine": {"exec": {sg.EXEC_PERSISTENT: "one persistent cooperative kernel per chunk",
                             sg.EXEC_GRAPH: "cuda graph of 2 kernels per step"}.get(
                                 info.exec_mode, "per-step launches"),
                    "propagation": ("event-driven CSR push" if tuned is None else
                                    f"autotuned: {tuned['ell']} projections dense ELL pull, "
                                    f"{tuned['csr']} event-driven CSR push (instance 0)"),
                    "exec_kernel": sg._lib.KERNEL_NAMES.get(info.step_kernel, "?"),
-                   "l2": "flushed (256 MiB write) between timed steps; the cell-state window "
-                         "kept in persisting L2 is not evicted by the flush (resident by design)",
-                   "l2_persist_bytes": info.l2_persist_bytes,
-                   "parallelism": f"replicas x{world}"},
+                   "l2_persist_bytes": info.l2_persist_bytes},
         "synaptic_events_per_s": events_all / (ms_max / 1000.0),
         "gpu_launches": launches,
         "e2e": e2e,

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "../../include/scaffold_gb300.h"
@@ -21,6 +22,23 @@ namespace sgb {
 namespace {
 
 constexpr unsigned kFullMask = 0xffffffffu;
+constexpr int kMaxDevices = 64;
+
+// SM count of the current device, queried once per device and cached (the
+// delivery kernels are sized by it on every call).
+std::atomic<int> g_sms[kMaxDevices];
+
+int device_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+  int v = g_sms[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      return 1;
+    g_sms[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 // Scratch layout: [0] active count, [64..] active cell ids (256-byte aligned).
 constexpr uint32_t kListOffset = 64;
@@ -44,6 +62,11 @@ __global__ void __launch_bounds__(kBlock) k_ops_push(const uint32_t* scratch,
                                                      const uint32_t* __restrict__ syn,
                                                      const void* __restrict__ w, int* ring,
                                                      uint32_t n, uint32_t slots, uint32_t slot0) {
+  // Ring slot of each delay field value d = 0..15: (step + d) % slots, exact
+  // for every delay the 4-bit field can hold, whatever the ring's size.
+  __shared__ uint32_t s_slot[16];
+  if (threadIdx.x < 16) s_slot[threadIdx.x] = (slot0 + threadIdx.x) % slots;
+  __syncthreads();
   const uint32_t n_act = scratch[0];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t nw = (gridDim.x * kBlock) >> 5;
@@ -54,8 +77,7 @@ __global__ void __launch_bounds__(kBlock) k_ops_push(const uint32_t* scratch,
       const uint32_t wd = __ldg(syn + q);
       const float wf = BF16 ? __uint_as_float(((uint32_t)__ldg((const unsigned short*)w + q)) << 16)
                             : __ldg((const float*)w + q);
-      uint32_t slot = slot0 + ((wd >> kPushPostBits) & 15u);
-      if (slot >= slots) slot -= slots;
+      const uint32_t slot = s_slot[(wd >> kPushPostBits) & 15u];
       atomicAdd(ring + (((size_t)slot * n + (wd & kPushPostMask)) << 1) + (wd >> 31),
                 __float2int_rn(wf));
     }
@@ -89,9 +111,7 @@ cudaError_t deliver_enqueue(const uint8_t* spikes, int32_t n_cells, const uint32
   const uint32_t n = (uint32_t)n_cells;
   k_ops_compact<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(spikes, n, scratch);
   if ((e = cudaGetLastError())) return e;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   const uint32_t slot0 = (uint32_t)(step % ring_slots);
   const int blocks = 2 * (sms > 0 ? sms : 1);
   if (weight_type == SGB_WEIGHT_BF16)
@@ -142,14 +162,15 @@ static __device__ __align__(256) uint32_t g_deliver_scratch[sgb::kListOffset + k
 namespace sgb {
 namespace {
 
-constexpr int kMaxDevices = 64;
-
 std::mutex g_scratch_mu;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the static scratch on the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is looked up
-// once per device, with that device current, and cached.
+// once per device, with that device current, and cached.  A cudaDeviceReset
+// ends the context that holds the array (as it frees every device buffer the
+// caller owns), so the cached address is stale after one: this entry point is
+// not for a device that the process has reset.
 int static_scratch(uint32_t** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

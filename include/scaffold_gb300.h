@@ -395,7 +395,10 @@ int sgb_sim_profile(sgb_sim* sim, int32_t n_steps, double* mean_us, double* byte
  *   post = syn[q] & (2^27 - 1), d = (syn[q] >> 27) & 15, a = syn[q] >> 31,
  *   ring[((step + d) % ring_slots) * n_cells + post][a] += rint(weights[q]),
  * where weights are FP32 or BF16 already multiplied by the accumulator's 2^S.
- * All pointers are device pointers; work is enqueued on `stream` (a
+ * Every delay field value 0..15 is taken modulo ring_slots, so a table whose
+ * delays reach ring_slots or beyond wraps around the ring (it never writes
+ * outside it); a simulation that needs every spike to land in its own future
+ * slot keeps all delays < ring_slots.  All pointers are device pointers; work is enqueued on `stream` (a
  * cudaStream_t as void*, NULL = legacy default stream) and the call returns
  * without waiting.  Scratch for the active-cell list is taken from the
  * stream-ordered pool (cudaMallocAsync) and released on the same stream. */
@@ -415,9 +418,12 @@ int sgb_deliver_spikes(const uint8_t* spikes, int32_t n_cells, const uint32_t* r
  * library holds until the process exits.  Larger n_cells return
  * SGB_ERR_RANGE.  The first call on a device looks up that array's device
  * address (cudaGetSymbolAddress) with the device current; make that first
- * call before any stream capture.  Every call clears the count word on its
- * stream and shares the one array, so calls that overlap on the GPU (other
- * streams, other host threads) race: serialise them. */
+ * call before any stream capture.  A cudaDeviceReset of that device ends the
+ * context holding the array, so the cached address is stale afterwards: do
+ * not call this entry point on a device the process has reset.  Every call
+ * clears the count word on its stream and shares the one array, so calls
+ * that overlap on the GPU (other streams, other host threads) race:
+ * serialise them. */
 int sgb_deliver_spikes_static(const uint8_t* spikes, int32_t n_cells, const uint32_t* row,
                               const uint32_t* syn, const void* weights, int32_t weight_type,
                               int32_t* ring, int32_t ring_slots, int64_t step, void* stream);

@@ -17,8 +17,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = os.environ.get("SGB_REFERENCE_DIR",
-                     "/root/reference/SimulationModule/Scaffold")
+# The reference's Scaffold directory: SGB_REFERENCE_DIR when set, else the
+# read-only checkout this recipe is written for.
+REF = os.environ.get("SGB_REFERENCE_DIR") or "/root/reference/SimulationModule/Scaffold"
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -110,6 +110,15 @@ int orc_plastic_values(const orc_sim* s, int32_t proj, float* values);
  * cells are left untouched).  Does not advance the simulation. */
 int orc_input_flags(const orc_sim* s, uint64_t t, uint8_t* flags);
 
+/* Synthetic benchmark networks (netgen.c): one fixed in-degree projection
+ * drawn from `seed` into caller arrays of npost * in_degree entries, and the
+ * scaffold architecture of configurations 1, 2 and 5. */
+int orc_random_projection(int64_t npre, int64_t npost, int32_t in_degree, float w_mean,
+                          float w_lo, float w_hi, int32_t d_min, int32_t d_max, uint64_t seed,
+                          uint32_t* pre_idx, uint32_t* post_idx, float* weight, uint8_t* delay);
+int orc_scaffold_spec(int32_t config, double scale, int32_t* sizes, int32_t* proj, float* drive,
+                      int32_t* burst_n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -236,6 +236,73 @@ def describe(net) -> dict:
     return dict(pops=pops, projs=projs, srcs=srcs, plast=plast)
 
 
+_LIF = dict(Cm=3.0, El=-70.0, dt_ref=2.0, Ie=0.0, Vr=-70.0, Vth=-50.0,
+            gL=float(np.float32(0.2)), channels=[(1.0, 0.0, 1.0, 0.5), (1.0, -80.0, 1.0, 10.0)])
+_INPUT = dict(Cm=0.0, El=0.0, dt_ref=0.0, Ie=0.0, Vr=0.0, Vth=0.0, gL=0.0, channels=[])
+
+
+def random_projection(npre, npost, in_degree, w_mean, seed, w_lo=0.5, w_hi=1.5, d_min=1,
+                      d_max=4):
+    """Fixed in-degree projection drawn by the oracle's generator (netgen.c):
+    (pre_idx, post_idx, weight, delay) arrays, post-major, pre ids ascending."""
+    L = lib()
+    L.orc_random_projection.argtypes = [C.c_int64, C.c_int64, C.c_int32, C.c_float, C.c_float,
+                                        C.c_float, C.c_int32, C.c_int32, C.c_uint64,
+                                        C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                        C.POINTER(C.c_float), C.POINTER(C.c_uint8)]
+    n = int(npost) * int(in_degree)
+    pre = np.empty(n, np.uint32)
+    post = np.empty(n, np.uint32)
+    w = np.empty(n, np.float32)
+    d = np.empty(n, np.uint8)
+    rc = L.orc_random_projection(npre, npost, in_degree, w_mean, w_lo, w_hi, d_min, d_max,
+                                 seed & 0xFFFFFFFFFFFFFFFF, _p(pre, C.c_uint32),
+                                 _p(post, C.c_uint32), _p(w, C.c_float), _p(d, C.c_uint8))
+    if rc:
+        raise RuntimeError(f"orc_random_projection failed ({rc})")
+    return pre, post, w, d
+
+
+def scaffold_desc(config: int, scale: float = 1.0, seed: int = 1) -> dict:
+    """Description (as `describe`) of benchmark scaffold `config` (1, 2 or 5)
+    at population scale `scale`, drawn from `seed` by the oracle's own
+    generator: the same network the library builds for these arguments,
+    without loading the library."""
+    L = lib()
+    L.orc_scaffold_spec.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                                    C.POINTER(C.c_int32)]
+    sizes = np.zeros(7, np.int32)
+    proj = np.zeros(44, np.int32)
+    drive = np.zeros(11, np.float32)
+    burst = C.c_int32()
+    if L.orc_scaffold_spec(config, scale, _p(sizes, C.c_int32), _p(proj, C.c_int32),
+                           _p(drive, C.c_float), C.byref(burst)):
+        raise ValueError(f"unknown scaffold config {config} or scale {scale}")
+    pops = [dict(num=int(sizes[0]), is_input=True, **_INPUT)]
+    pops += [dict(num=int(n), is_input=False, **_LIF) for n in sizes[1:]]
+    projs = []
+    for j in range(11):
+        pre, post, k, ch = (int(x) for x in proj[4 * j: 4 * j + 4])
+        mean = float(drive[j] / np.float32(k)) if k > 0 else 0.0
+        pj_seed = (seed * 1000003 + j + 1) & 0xFFFFFFFFFFFFFFFF
+        a, b, w, d = random_projection(int(sizes[pre]), int(sizes[post]), k, mean, pj_seed)
+        projs.append(dict(pre=pre, post=post, channel=ch, pre_idx=a, post_idx=b, weight=w,
+                          delay=d))
+    srcs = [dict(pop=0, ids=np.arange(sizes[0], dtype=np.uint32), kind=0, rate_hz=4.0,
+                 phase_ms=0.0, win_period_ms=0.0, win_start_ms=0.0, win_end_ms=0.0)]
+    if burst.value:
+        srcs.append(dict(pop=0, ids=np.arange(burst.value, dtype=np.uint32), kind=0,
+                         rate_hz=100.0, phase_ms=0.0, win_period_ms=1000.0, win_start_ms=260.0,
+                         win_end_ms=300.0))
+    return dict(pops=pops, projs=projs, srcs=srcs, plast=[])
+
+
+def desc_counts(desc: dict):
+    """(cells, synapses) of a description."""
+    return (sum(p["num"] for p in desc["pops"]), sum(len(p["pre_idx"]) for p in desc["projs"]))
+
+
 REF_DIR = os.path.join(HERE, "_ref")
 
 

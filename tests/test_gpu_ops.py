@@ -55,6 +55,16 @@ def expected(ring, n, row, syn, wsc, spikes, step, slots):
             ring[(step + dl) % slots, post, ch] += int(np.rint(wsc[q]))
 
 
+def test_ring_wrap_restatement_cpu():
+    """The restatement's slot rule for delays at or beyond the ring size: a
+    delay-4 synapse on a 3-slot ring at step 1 lands in slot (1 + 4) % 3 = 2."""
+    ring = np.zeros((3, 2, 2), np.int64)
+    row = np.array([0, 1, 1], np.uint32)
+    syn = np.array([1 | (4 << 27)], np.uint32)
+    expected(ring, 2, row, syn, np.array([7.0], np.float32), np.array([1, 0], np.uint8), 1, 3)
+    assert ring[2, 1, 0] == 7 and ring.sum() == 7
+
+
 def test_push_table_helper_cpu():
     """The restatement used by the GPU checks covers every synapse once (no GPU)."""
     net = sg.scaffold(1, 0.25, 17)
@@ -66,13 +76,15 @@ def test_push_table_helper_cpu():
 
 
 @gpu
-@pytest.mark.parametrize("bf16", [False, True])
-def test_deliver_spikes_matches_restatement(bf16):
+@pytest.mark.parametrize("bf16,slots", [(False, 5), (True, 5), (False, 2), (True, 3)])
+def test_deliver_spikes_matches_restatement(bf16, slots):
+    """slots 2 and 3 are below the table's largest delay (4): those synapses
+    wrap around the ring, (step + d) % slots, and stay inside it."""
     import torch
 
     net = sg.scaffold(1, 0.25, 17)
     n, row, syn, wsc = push_table(net, bf16)
-    slots = 5
+    assert int(((syn >> 27) & 15).max()) == 4
     dev = torch.device("cuda")
     t_row = torch.from_numpy(row.view(np.int32)).to(dev)
     t_syn = torch.from_numpy(syn.view(np.int32)).to(dev)

@@ -171,3 +171,28 @@ def test_scaffold_deterministic_and_scaled():
     assert len(set(scales)) == 64
     with pytest.raises(SgbError):
         sg.Network().build_scaffold(3)
+
+
+@pytest.mark.parametrize("config,scale,seed", [(1, 1.0, 1), (2, 1.0, 1), (2, 0.41, 23),
+                                               (1, 0.25, 7), (5, 0.05, 3)])
+def test_oracle_generator_draws_the_library_networks(config, scale, seed):
+    """The oracle's own generator (oracle/netgen.c), which the CPU arms of the
+    benchmark use so that they load no library code, draws exactly the
+    library's synthetic scaffolds: populations, every synapse array and the
+    stimulus sources."""
+    import oracle_py
+
+    a = oracle_py.describe(sg.scaffold(config, scale, seed))
+    b = oracle_py.scaffold_desc(config, scale, seed)
+    assert a["pops"] == b["pops"]
+    assert len(a["projs"]) == len(b["projs"]) == 11
+    for pa, pb in zip(a["projs"], b["projs"]):
+        assert (pa["pre"], pa["post"], pa["channel"]) == (pb["pre"], pb["post"], pb["channel"])
+        for k in ("pre_idx", "post_idx", "weight", "delay"):
+            assert pa[k].dtype == pb[k].dtype
+            assert np.array_equal(pa[k].view(np.uint8), pb[k].view(np.uint8)), k
+    assert len(a["srcs"]) == len(b["srcs"])
+    for sa, sb in zip(a["srcs"], b["srcs"]):
+        assert np.array_equal(sa["ids"], sb["ids"])
+        assert {k: v for k, v in sa.items() if k != "ids"} == \
+            {k: v for k, v in sb.items() if k != "ids"}

@@ -25,13 +25,14 @@ from test_gpu_ops import bf16_bits, push_table  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("bf16", [False, True])
-def test_static_scratch_matches_allocating_entry_point(bf16):
+@pytest.mark.parametrize("bf16,slots", [(False, 5), (True, 5), (False, 3)])
+def test_static_scratch_matches_allocating_entry_point(bf16, slots):
+    """slots 3 is below the table's largest delay (4): those synapses wrap
+    around the ring in both entry points alike."""
     import torch
 
     net = sg.scaffold(1, 0.25, 23)
     n, row, syn, wsc = push_table(net, bf16)
-    slots = 5
     dev = torch.device("cuda")
     t_row = torch.from_numpy(row.view(np.int32)).to(dev)
     t_syn = torch.from_numpy(syn.view(np.int32)).to(dev)
