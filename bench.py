@@ -294,6 +294,92 @@ def plasticity_leg(peak: float, bench_steps: int = 5, chunk: int = 1000):
             "k_deliver_us": mean_us[1]}
 
 
+def step_bytes(sim, pull_entries: int) -> int:
+    """Algorithmic bytes of one exchange step's update phase: per LIF cell
+    12 B state read + 12 B write + 8 B ring slot; per input cell 4 B source
+    mask; 8 B per 32-cell bitmap word (two history copies); 4 B per dense
+    entry streamed."""
+    import scaffold_gb300 as sg
+
+    segs = sim.segments()
+    n_lif = sum(x.count for x in segs if x.dev_type != sg.INPUT)
+    n_in = sum(x.count for x in segs if x.dev_type == sg.INPUT)
+    n_words = sum((x.count + 31) // 32 for x in segs)
+    return 32 * n_lif + 4 * n_in + 8 * n_words + 4 * pull_entries
+
+
+def traffic_of(workload: str, kernel: str):
+    """ncu DRAM bytes per launch (profiles/traffic.json) or None."""
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(tp)).get(workload, {}).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def config4_leg(peak: float, bench_steps: int = 5, chunk: int = 1000):
+    """Config 4, the batched form: 64 instances of the config-2 architecture,
+    sizes scaled U[0.25, 2.0) from each instance's seed, BF16 tables, one
+    persistent launch per 1,000-step chunk, L2 flushed before every timed
+    launch.  Realtime factor over all instances, and the roofline of the
+    launch twice: on algorithmic bytes (which count the cell state that the
+    persisting L2 window serves) and on the DRAM bytes one ncu capture
+    measured (profiles/traffic.json), which do not."""
+    import torch
+
+    import scaffold_gb300 as sg
+
+    seeds = [1 + k for k in range(64)]
+    nets = [sg.scaffold(2, sc, sd) for sc, sd in zip(sg.batched_scales(seeds), seeds)]
+    sim = sg.Simulation(nets, seeds, weight_type=sg.WEIGHT_BF16, chunk_steps=chunk,
+                        exec_mode=sg.EXEC_PERSISTENT)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        sim.enqueue(chunk)
+    sim.sync()
+    info0 = sim.info()
+    evs = []
+    for i in range(bench_steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.enqueue(chunk)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    sim.sync()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    info = sim.info()
+    kname = sg._lib.KERNEL_NAMES.get(info.step_kernel, "?")
+    alg = (bench_steps * chunk * step_bytes(sim, info.pull_entries) +
+           (info.delivered - info0.delivered) * (12 + 2) + (info.pulled - info0.pulled) * (8 + 2))
+    launch_s = ms / 1000.0 / bench_steps
+    achieved = alg / bench_steps / launch_s / 1e9
+    dram = traffic_of("c4", kname)
+    dram_gbs = dram / launch_s / 1e9 if dram else None
+    out = {"workload": f"config 4: 64 instances, {info.n_neurons} cells, {info.n_synapses} "
+                       f"synapses, BF16, sizes scaled U[0.25, 2.0)",
+           "exec_kernel": kname, "realtime_factor": len(nets) * bench_steps * chunk * 1e-4 /
+           (ms * 1e-3), "us_per_step": 1000.0 * ms / (bench_steps * chunk),
+           "synaptic_events_per_s": (info.events - info0.events) / (ms * 1e-3),
+           "launches_timed": bench_steps, "steps_per_launch": chunk,
+           "roofline_algorithmic": {"achieved": achieved, "peak": peak, "unit": "GB/s",
+                                    "frac": achieved / peak,
+                                    "bytes_per_launch": alg / bench_steps},
+           "roofline_dram": {"achieved": dram_gbs, "peak": peak, "unit": "GB/s",
+                             "frac": dram_gbs / peak if dram_gbs else None,
+                             "bytes_per_launch": dram,
+                             "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "launch (profiles/traffic.json)"},
+           "l2": "flushed (256 MiB write) before every timed launch; the cell state in the "
+                 "persisting L2 window is exempt"}
+    sim.close()
+    return out
+
+
 def ell_roofline(peak: float):
     """Dense ELL pull at HBM scale: config 5 (4 batched seeds of the ~925k-cell
     scaffold, 109M synapses, 437 MB of ELL entries, larger than L2) with every
@@ -315,13 +401,7 @@ def ell_roofline(peak: float):
     sim.close()
     gbs = bytes_pl[2] / (mean_us[2] * 1e-6) / 1e9
     ceiling = stream_copy_gbs(int(info.pull_entries) * 4)
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get("dense_ell", {}).get("k_pull")
-        except ValueError:
-            traffic = None
+    traffic = traffic_of("dense_ell", "k_pull")
     return {"kernel": "k_pull (dense ELL pull, every projection)", "traffic": traffic, "workload":
             f"config 5: 4 seeds, {info.n_neurons} cells, {info.n_synapses} synapses, BF16",
             "mean_us": mean_us[2], "bytes_per_launch": bytes_pl[2], "achieved": gbs,
@@ -491,25 +571,15 @@ def run_gb300(a):
     # copies); per delivered push synapse 4 B word + W B weight + 8 B atomic
     # read-modify-write; per dense entry and step 4 B, plus W + 8 B per entry
     # whose pre cell spiked.
-    segs = sim.segments()
-    n_lif = sum(sg_.count for sg_ in segs if sg_.dev_type != sg.INPUT)
-    n_in = sum(sg_.count for sg_ in segs if sg_.dev_type == sg.INPUT)
-    n_words = sum((sg_.count + 31) // 32 for sg_ in segs)
     wbytes = 2 if wl["bf16"] else 4
     info1 = sim.info()
-    upd_step = 32 * n_lif + 4 * n_in + 8 * n_words + 4 * info_t.pull_entries
+    upd_step = step_bytes(sim, info_t.pull_entries)
     alg_bytes = (a.steps * a.chunk * upd_step + (dlv1 - dlv0) * (12 + wbytes) +
                  (info_t.pulled - pull0) * (8 + wbytes))
     peak, peak_kind = measured_hbm()
     achieved = alg_bytes / (ms / 1000.0) / 1e9
     kname = sg._lib.KERNEL_NAMES.get(info1.step_kernel, "?")
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get(a.workload, {}).get(kname)
-        except ValueError:
-            traffic = None
+    traffic = traffic_of(a.workload, kname)
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
             "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes / a.steps,
@@ -531,6 +601,7 @@ def run_gb300(a):
               if c > 0}
     ell = None if a.no_ell_roofline else ell_roofline(peak)
     plast = None if a.no_ell_roofline else plasticity_leg(peak)
+    c4 = None if (a.no_ell_roofline or a.workload != "c2") else config4_leg(peak)
     cpu = None
     c1 = None
     if not a.no_cpu_baseline:
@@ -562,6 +633,7 @@ def run_gb300(a):
         "phase_profile": phases,
         "dense_ell_roofline": ell,
         "plasticity": plast,
+        "config4": c4,
         "config1": c1,
         "cpu_baseline": cpu,
         "clocks": clk,

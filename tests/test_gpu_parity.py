@@ -339,23 +339,3 @@ def test_general_kernel_block_item_overflow(delay):
     assert counts[:, 0].sum() == n_src * steps and counts[:, 1].sum() > 0
     assert sim.info().delivered == exp[6]
     sim.close()
-
-
-def test_many_segments_fall_back_to_global_descriptors():
-    """250 batched instances (1,750 segments): the persistent kernels' copy of
-    the segment descriptors no longer fits in shared memory, so the general
-    kernel reads them from global memory; counts and state equal the
-    per-step driver's bit for bit."""
-    seeds = list(range(1, 251))
-    nets = [sg.scaffold(1, 0.1, sd) for sd in seeds]
-    steps = 120
-    a = sg.Simulation(nets, seeds, exec_mode=sg.EXEC_PERSISTENT, chunk_steps=60)
-    assert a.info().step_kernel == 1  # SGB_KERNEL_GENERAL
-    b = sg.Simulation(nets, seeds, exec_mode=sg.EXEC_GRAPH, chunk_steps=60)
-    ca, _ = a.loop_n_steps(steps)
-    cb, _ = b.loop_n_steps(steps)
-    assert ca.sum() > 0 and np.array_equal(ca, cb)
-    for x, y in zip(a.state(), b.state()):
-        assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32))
-    a.close()
-    b.close()
