@@ -20,7 +20,10 @@
 // per chunk of steps (a bounded grid barrier orders them).  The persistent
 // kernel comes in three forms: fused (every word resident in one warp, every
 // projection event-driven: update and push share one phase, one barrier a
-// step, push rows and items in shared memory), resident (words resident,
+// step, push rows and items in shared memory; with one substep a step it
+// publishes each step's spikes one step early, as soon as the potential
+// that decides them is known, and reads every ring slot a step ahead of its
+// use), resident (words resident,
 // some dense pulls: two barriers) and general (more words than warps; one
 // barrier a step with the pushes in each block's shared memory when every
 // projection is event-driven, else two with a global item list).  With
@@ -1262,7 +1265,8 @@ __device__ __forceinline__ uint32_t push_any(const StepArgs& a, const uint2* row
   return (it.y & 1u) ? push_item_smem(a, rows, it, s0) : push_item<BF16>(a, it, s0);
 }
 
-template <bool BF16>
+// AHEAD: the spike-ahead timeline of one-substep steps (see the loop below).
+template <bool BF16, bool AHEAD>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs a,
                                                                        uint32_t n_steps) {
   __shared__ uint2 s_items[kBlockItems];
@@ -1416,79 +1420,81 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   bool aborted = false;
   if (threadIdx.x == 0) s_n[0] = s_n[1] = 0;
   __syncthreads();
-  for (uint32_t s = 0; s < n_steps; ++s) {
-    ix.t = t0 + s;
-    ix.rel = s;
-    const uint32_t par = s & 1u;
-    clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
-    // Shards of the previous step's spikes (none at a launch's first step:
-    // each launch pushes its last step's shards itself, after the loop).
-    const bool sh_ck = s > 0 && threadIdx.x < n_sh;
-    const uint32_t sh_w =
-        sh_ck ? __ldcg(hist_base(a, ix.hrow) + a.n_words + (s_sh[threadIdx.x].x >> 5)) : 0u;
-    uint32_t off = 0, nit = 0;
-    if (has) {
-      const bool fired = lif ? cell_fire(a, segs[seg], i, 0u, valid, st, 0u, ix) : next_in;
-      const uint32_t ballot = __ballot_sync(kFull, fired);
-      if (lane == 0) put_hist(a, ix, w, ballot);
-      if (ballot) {
-        const uint32_t n = __popc(ballot);
-        const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
-        const uint32_t ev = __reduce_add_sync(kFull, fired ? s_od[threadIdx.x] : 0u);
-        nit = fired ? ((rl & 0x7FFFFFFFu) + kFusedChunk - 1) / kFusedChunk : 0u;
-        uint32_t incl = nit;
+  // off / nit: the lane's first item in the block's list and its item count
+  // (a warp delivers its own items past the list's capacity).
+  uint32_t off = 0, nit = 0;
+  // Spike bookkeeping of this warp's word for the spikes of step px.t (chunk
+  // row `rel`): history and summary bits, per-segment count, events, raster
+  // entries, and the spiking cells' rows cut into kFusedChunk-synapse items
+  // in the block's list of parity `par`.
+  auto publish = [&](bool fired, const StepIdx& px, uint32_t rel, uint32_t par) {
+    off = 0;
+    nit = 0;
+    const uint32_t ballot = __ballot_sync(kFull, fired);
+    if (lane == 0) put_hist(a, px, w, ballot);
+    if (!ballot) return;
+    const uint32_t n = __popc(ballot);
+    const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
+    const uint32_t ev = __reduce_add_sync(kFull, fired ? s_od[threadIdx.x] : 0u);
+    nit = fired ? ((rl & 0x7FFFFFFFu) + kFusedChunk - 1) / kFusedChunk : 0u;
+    uint32_t incl = nit;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t v = __shfl_up_sync(kFull, incl, o);
-          if (lane >= (uint32_t)o) incl += v;
-        }
-        const uint32_t tot = __shfl_sync(kFull, incl, 31);
-        uint32_t roff = 0;
-        if (lane == 0) {
-          if (tot) off = atomicAdd(&s_n[par], tot);
-          atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], n);
-          if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
-          if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
-        }
-        off = __shfl_sync(kFull, off, 0) + incl - nit;
-        for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
-          const uint32_t q = k * kFusedChunk;
-          s_items[off + k] = make_uint2(qb + q, (min(kFusedChunk, (rl & 0x7FFFFFFFu) - q) << 23) |
-                                                    (rl >> 31));
-        }
-        if (a.raster_cap) {
-          roff = __shfl_sync(kFull, roff, 0);
-          if (fired) {
-            if (roff + rank < a.raster_cap)
-              a.raster[roff + rank] = i;
-            else
-              atomicOr(&ctl->error, kErrRasterOverflow);
-          }
-        }
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(kFull, incl, o);
+      if (lane >= (uint32_t)o) incl += v;
+    }
+    const uint32_t tot = __shfl_sync(kFull, incl, 31);
+    uint32_t roff = 0;
+    if (lane == 0) {
+      if (tot) off = atomicAdd(&s_n[par], tot);
+      atomicAdd(&a.counts[(size_t)rel * a.n_segs + seg], n);
+      if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
+      if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, n);
+    }
+    off = __shfl_sync(kFull, off, 0) + incl - nit;
+    for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
+      const uint32_t q = k * kFusedChunk;
+      s_items[off + k] = make_uint2(qb + q, (min(kFusedChunk, (rl & 0x7FFFFFFFu) - q) << 23) |
+                                                (rl >> 31));
+    }
+    if (a.raster_cap) {
+      roff = __shfl_sync(kFull, roff, 0);
+      if (fired) {
+        if (roff + rank < a.raster_cap)
+          a.raster[roff + rank] = i;
+        else
+          atomicOr(&ctl->error, kErrRasterOverflow);
       }
     }
-    // A spiking shard becomes kFusedChunk-synapse items; those past the
-    // list's capacity (from item sh_from on) its thread's warp pushes below.
-    uint32_t sh_from = kNoRow;
-    if (sh_ck) {
+  };
+  // A spiking shard (its cell's bit set in the history word sh_w) becomes
+  // kFusedChunk-synapse items of parity par; returns the first item past the
+  // list's capacity, which this thread's warp pushes itself (kNoRow: none).
+  auto shard_items = [&](bool ck, uint32_t sh_w, uint32_t par) -> uint32_t {
+    uint32_t from = kNoRow;
+    if (ck) {
       const uint4 h = s_sh[threadIdx.x];
       if ((sh_w >> (h.x & 31u)) & 1u) {
-        const uint32_t len = h.z >> 23, ni = (len + kFusedChunk - 1) / kFusedChunk;
+        const uint32_t sl = h.z >> 23, ni = (sl + kFusedChunk - 1) / kFusedChunk;
         const uint32_t o = atomicAdd(&s_n[par], ni);
         for (uint32_t k = 0; k < ni && o + k < kBlockItems; ++k)
           s_items[o + k] = make_uint2(h.y + k * kFusedChunk,
-                                      (min(kFusedChunk, len - k * kFusedChunk) << 23) | (h.z & 3u));
-        if (o + ni > kBlockItems) sh_from = o < kBlockItems ? kBlockItems - o : 0u;
+                                      (min(kFusedChunk, sl - k * kFusedChunk) << 23) | (h.z & 3u));
+        if (o + ni > kBlockItems) from = o < kBlockItems ? kBlockItems - o : 0u;
       }
     }
+    return from;
+  };
+  // The block's items of parity par, then the items past the list's
+  // capacity; own rows count their delays from ring slot `own`, shards from
+  // ring slot `shard` (their spike's step).
+  auto deliver = [&](uint32_t par, uint32_t own, uint32_t shard, uint32_t sh_from) {
     __syncthreads();
     const uint32_t n_items = min(s_n[par], kBlockItems);
-    // The other parity's count was last read before this step's __syncthreads.
+    // The other parity's count was last read before this __syncthreads.
     if (threadIdx.x == 0) s_n[par ^ 1u] = 0;
-    const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
     for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32)
-      walked += push_any<BF16>(a, s_rows, s_items[u], ix.slot, prev);
-    // Items beyond the block's capacity are delivered by the warp that made them.
+      walked += push_any<BF16>(a, s_rows, s_items[u], own, shard);
     uint32_t spill = __ballot_sync(kFull, off + nit > kBlockItems);
     while (spill) {
       const int src = __ffs(spill) - 1;
@@ -1498,7 +1504,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       for (uint32_t k = o < kBlockItems ? kBlockItems - o : 0; k < c; ++k) {
         const uint32_t q = k * kFusedChunk;
         const uint2 it = make_uint2(b0 + q, (min(kFusedChunk, (bl & 0x7FFFFFFFu) - q) << 23) | (bl >> 31));
-        walked += push_any<BF16>(a, s_rows, it, ix.slot, prev);
+        walked += push_any<BF16>(a, s_rows, it, own, shard);
       }
     }
     if (n_sh) {
@@ -1507,39 +1513,148 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         const int src = __ffs(sp) - 1;
         sp &= sp - 1;
         const uint4 h = s_sh[wib * 32u + src];
-        const uint32_t len = h.z >> 23;
-        for (uint32_t q = __shfl_sync(kFull, sh_from, src) * kFusedChunk; q < len; q += kFusedChunk)
+        const uint32_t sl = h.z >> 23;
+        for (uint32_t q = __shfl_sync(kFull, sh_from, src) * kFusedChunk; q < sl; q += kFusedChunk)
           walked += push_any<BF16>(
-              a, s_rows, make_uint2(h.y + q, (min(kFusedChunk, len - q) << 23) | (h.z & 3u)), ix.slot,
-              prev);
+              a, s_rows, make_uint2(h.y + q, (min(kFusedChunk, sl - q) << 23) | (h.z & 3u)), own,
+              shard);
       }
     }
-    grid_arrive(a, target);
-    if (stim && s + 1 < n_steps)
-      next_in = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1);
-    if (!grid_wait(a, target, s_poller)) {
-      aborted = true;
-      break;
+  };
+  if (!AHEAD) {
+    // Step t: update (ring slot t), spikes of t, their pushes and the shards
+    // of step t - 1's spikes; one grid barrier.
+    for (uint32_t s = 0; s < n_steps; ++s) {
+      ix.t = t0 + s;
+      ix.rel = s;
+      const uint32_t par = s & 1u;
+      clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
+      // Shards of the previous step's spikes (none at a launch's first step:
+      // each launch pushes its last step's shards itself, after the loop).
+      const bool sh_ck = s > 0 && threadIdx.x < n_sh;
+      const uint32_t sh_w =
+          sh_ck ? __ldcg(hist_base(a, ix.hrow) + a.n_words + (s_sh[threadIdx.x].x >> 5)) : 0u;
+      off = nit = 0;
+      if (has) {
+        const bool fired = lif ? cell_fire(a, segs[seg], i, 0u, valid, st, 0u, ix) : next_in;
+        publish(fired, ix, s, par);
+      }
+      const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
+      deliver(par, ix.slot, ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u, sh_from);
+      grid_arrive(a, target);
+      if (stim && s + 1 < n_steps)
+        next_in = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1);
+      if (!grid_wait(a, target, s_poller)) {
+        aborted = true;
+        break;
+      }
+      ix_advance(a, ix);
     }
-    ix_advance(a, ix);
+    // The shards of the last step's spikes (ix has advanced past that step).
+    if (!aborted && n_sh && n_steps) {
+      const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
+      bool hit = false;
+      if (threadIdx.x < n_sh) {
+        const uint32_t c = s_sh[threadIdx.x].x;
+        hit = (__ldcg(hist_base(a, ix.hrow) + a.n_words + (c >> 5)) >> (c & 31u)) & 1u;
+      }
+      uint32_t sp = __ballot_sync(kFull, hit);
+      while (sp) {
+        const int src = __ffs(sp) - 1;
+        sp &= sp - 1;
+        const uint4 h = s_sh[wib * 32u + src];
+        walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
+      }
+    }
+  } else {
+    // Spike-ahead timeline (one substep per step).  A cell's spike of step
+    // t + 1 is decided by its potential after the update of step t (the spike
+    // test reads the potential before the step's integration), so step t
+    // updates with ring slot t, then publishes and pushes the spikes of
+    // t + 1 and the shards of t's spikes.  Every push into ring slot t + 1 is
+    // then made by the end of step t - 1, so the slot is read at the start of
+    // step t, a whole step ahead of its use: the step's critical path has no
+    // ring read.  A prologue publishes and pushes the spikes of the launch's
+    // first step; the last step publishes nothing and leaves its next slot
+    // unread, so a launch ends in the same state as with the other timeline.
+    // The ring slot a LIF word consumes next is staged in shared memory by
+    // asynchronous 16-byte copies at L2 (cp.async.cg: never a stale L1 line),
+    // so no registers are held for it across the pushes and the barrier.
+    __shared__ __align__(16) int2 s_acc[kPersistBlock];
+    int2* ring2 = reinterpret_cast<int2*>(a.ring);
+    const bool rd = has && lif && valid;
+    const bool fetch = has && lif;  // warp-uniform
+    auto fetch_slot = [&](uint32_t roff) {  // lanes 0..15: two cells each
+      if (lane < 16u) {
+        const int2* src = ring2 + (roff + (w << 5) + 2u * lane);
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_acc[(wib << 5) + 2u * lane]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    // After the warp's copies landed: the fetched entries, cleared in the ring.
+    auto clear_slot = [&](uint32_t roff) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      __syncwarp();
+      const int2 v = s_acc[threadIdx.x];
+      if (rd && (v.x | v.y)) __stcg(ring2 + (roff + i), make_int2(0, 0));
+    };
+    bool in_next = false;  // input spike of step t + 1, drawn a step ahead
+    if (n_steps) {
+      if (fetch) fetch_slot(ix.roff);
+      if (stim && n_steps > 1)
+        in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), t0 + 1);
+      ix.rel = 0;
+      clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
+      off = nit = 0;
+      if (has) publish(valid && (lif ? st.x > segs[seg].Vth : next_in), ix, 0u, 0u);
+      deliver(0u, ix.slot, ix.slot, kNoRow);
+      if (fetch) clear_slot(ix.roff);
+      grid_arrive(a, target);
+      aborted = !grid_wait(a, target, s_poller);
+    }
+    for (uint32_t s = 0; s < n_steps && !aborted; ++s) {
+      StepIdx nx = ix;
+      nx.t = ix.t + 1ull;
+      nx.rel = s + 1u;
+      ix_advance(a, nx);
+      const bool more = s + 1u < n_steps;
+      const uint32_t par = (s + 1u) & 1u;
+      // Shards of this step's spikes: their cells' bits in the history row of t.
+      const bool sh_ck = threadIdx.x < n_sh;
+      const uint32_t sh_w = sh_ck ? __ldcg(hist_base(a, ix.hrow) + (s_sh[threadIdx.x].x >> 5)) : 0u;
+      const uint32_t shard_slot = ix.slot;
+      ix = nx;  // from here on: step t + 1, whose spikes this step publishes
+      clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x,
+                         gridDim.x * kPersistBlock);  // the row of step t + 2
+      off = nit = 0;
+      if (has) {
+        bool fired = false;
+        if (lif) {
+          const LifK k = lif_k(segs[seg]);
+          if (rd) lif_update<1>(k, 1, st, s_acc[threadIdx.x]);
+          fired = valid && st.x > k.Vth;
+          // Ring slot t + 1: complete since the last grid barrier; its copy
+          // lands while the block pushes.
+          if (more) fetch_slot(ix.roff);
+        } else {
+          fired = in_next;
+        }
+        if (more) publish(fired, ix, s + 1u, par);
+      }
+      const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
+      deliver(par, ix.slot, shard_slot, sh_from);
+      if (fetch && more) clear_slot(ix.roff);
+      grid_arrive(a, target);
+      if (stim && s + 2u < n_steps)
+        in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
+      if (!grid_wait(a, target, s_poller)) {
+        aborted = true;
+        break;
+      }
+    }
   }
   if (valid && lif) state_out(a, i, st);
-  // The shards of the last step's spikes (ix has advanced past that step).
-  if (!aborted && n_sh && n_steps) {
-    const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
-    bool hit = false;
-    if (threadIdx.x < n_sh) {
-      const uint32_t c = s_sh[threadIdx.x].x;
-      hit = (__ldcg(hist_base(a, ix.hrow) + a.n_words + (c >> 5)) >> (c & 31u)) & 1u;
-    }
-    uint32_t sp = __ballot_sync(kFull, hit);
-    while (sp) {
-      const int src = __ffs(sp) - 1;
-      sp &= sp - 1;
-      const uint4 h = s_sh[wib * 32u + src];
-      walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
-    }
-  }
   if (a.raster_cap && blockIdx.x == 0) raster_offsets_from_counts(a, n_steps, s_wsum);
   if (__ldcg(&ctl->error) & kErrBarrierTimeout) return;
   if (lane == 0 && walked) atomicAdd(&ctl->delivered, (unsigned long long)walked);
@@ -1648,12 +1763,18 @@ int persistent_blocks_per_sm(bool bf16) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<true, true>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<true, true>, kPersistBlock, 0);
+    int g = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g, k_persistent_fused<true, false>, kPersistBlock, 0);
+    f = f < g ? f : g;
   } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<false, true>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<false>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<false, true>, kPersistBlock, 0);
+    int g = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g, k_persistent_fused<false, false>, kPersistBlock, 0);
+    f = f < g ? f : g;
   }
   n = n < m ? n : m;
   n = n < o ? n : o;
@@ -1679,8 +1800,11 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
   const int kind = persistent_kernel_kind(a, blocks);
   const bool resident = kind != SGB_KERNEL_GENERAL;
   const bool fused = kind == SGB_KERNEL_FUSED;
-  const void* fn = fused      ? (a.bf16 ? (const void*)k_persistent_fused<true>
-                                        : (const void*)k_persistent_fused<false>)
+  const bool ahead = a.substeps == 1;
+  const void* fn = fused      ? (a.bf16 ? (ahead ? (const void*)k_persistent_fused<true, true>
+                                                 : (const void*)k_persistent_fused<true, false>)
+                                        : (ahead ? (const void*)k_persistent_fused<false, true>
+                                                 : (const void*)k_persistent_fused<false, false>))
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
                                         : (const void*)k_persistent_resident<false>)
                    : general_one_barrier(a)
@@ -1697,20 +1821,30 @@ uint32_t fused_row_smem_max() {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  cudaFuncAttributes fa{};
-  cudaFuncGetAttributes(&fa, k_persistent_fused<false>);
-  cudaFuncAttributes fb{};
-  cudaFuncGetAttributes(&fb, k_persistent_fused<true>);
-  const size_t st = fa.sharedSizeBytes > fb.sharedSizeBytes ? fa.sharedSizeBytes : fb.sharedSizeBytes;
+  size_t st = 0;
+  const void* fns[] = {(const void*)k_persistent_fused<false, false>,
+                       (const void*)k_persistent_fused<false, true>,
+                       (const void*)k_persistent_fused<true, false>,
+                       (const void*)k_persistent_fused<true, true>};
+  for (const void* fn : fns) {
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, fn);
+    st = fa.sharedSizeBytes > st ? fa.sharedSizeBytes : st;
+  }
   return (size_t)optin > st ? (uint32_t)(((size_t)optin - st) & ~(size_t)255) : 0u;
 }
 
 cudaError_t set_fused_row_smem(uint32_t bytes) {
-  cudaError_t e = cudaFuncSetAttribute(k_persistent_fused<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e) return e;
-  return cudaFuncSetAttribute(k_persistent_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)bytes);
+  const void* fns[] = {(const void*)k_persistent_fused<false, false>,
+                       (const void*)k_persistent_fused<false, true>,
+                       (const void*)k_persistent_fused<true, false>,
+                       (const void*)k_persistent_fused<true, true>};
+  for (const void* fn : fns) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace sgb

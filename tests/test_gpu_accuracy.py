@@ -1,12 +1,23 @@
 """Config 3 accuracy: BF16 synapse weights and FP32 state against the FP64 oracle.
 
-On the 92,550-cell scaffold the GPU raster (FP32 and BF16 tables) is compared
-with the FP64 oracle's: first step whose spike sets differ, fraction of the
-oracle's spikes reproduced by the same cell within +-1 step, and the relative
-firing-rate error of every population.  The FP32 path is additionally
-bit-identical to the FP32 oracle.  Set SGB_ACCURACY_OUT to a path to record
-the numbers as JSON.
+Config 3 is the 92,550-cell config-2 scaffold (seed 1) over its full 10 s of
+biological time (100,000 exchange steps of 0.1 ms).  The FP64 oracle's spike
+counts over those 10 s come from tests/golden/c3_rates_s1.json (written by
+make_c3_golden.py beside it), together with the FP32 oracle's counts and
+final state for FP32 and BF16 tables.  The tests check:
+
+  * the GPU path with FP32 tables and with BF16 tables is bit-identical to
+    the FP32 oracle in the same table mode over all 100,000 steps (every
+    step's population counts, and the complete final state);
+  * every population's firing rate over the 10 s is within 1 % of the FP64
+    oracle's, for FP32 and for BF16 tables;
+  * spike timing against a live FP64 oracle run over the first 4,000 steps:
+    first divergent step and the fraction of spikes reproduced by the same
+    cell within +-1 step.
+
+Set SGB_ACCURACY_OUT to a path to record the numbers as JSON.
 """
+import hashlib
 import json
 import os
 
@@ -18,10 +29,69 @@ import scaffold_gb300 as sg
 
 pytestmark = pytest.mark.gpu
 
-STEPS = 4000  # 0.4 s of biological time (includes the 260-300 ms mossy burst)
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c3_rates_s1.json")
+WEIGHTS = {"fp32": sg.WEIGHT_FP32, "bf16": sg.WEIGHT_BF16}
+TIMING_STEPS = 4000  # 0.4 s, includes the 260-300 ms mossy burst
+RATE_TOL = 0.01      # relative firing-rate error bound per population
 
 
-def _match_within_one(ids_a, off_a, ids_b, off_b, n_cells):
+def _state_digest(u, g, ref) -> str:
+    h = hashlib.sha256()
+    for a in (u, g, ref):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+_runs = {}
+
+
+def _ten_seconds(name):
+    """GPU run of config 3 over the fixture's steps with `name` tables:
+    (per-chunk population counts, SHA-256 of every step's counts, state digest)."""
+    if name not in _runs:
+        fx = json.load(open(GOLDEN))
+        net = sg.scaffold(fx["config"], fx["scale"], fx["seed"])
+        sim = sg.Simulation([net], [fx["seed"]], weight_type=WEIGHTS[name],
+                            exec_mode=sg.EXEC_PERSISTENT, chunk_steps=fx["chunk"])
+        h = hashlib.sha256()
+        chunks = []
+        for _ in range(fx["steps"] // fx["chunk"]):
+            c, _ = sim.loop_n_steps(fx["chunk"], counts=True)
+            c = np.ascontiguousarray(c, dtype="<u4")
+            h.update(c.tobytes())
+            chunks.append(c.sum(0).astype(np.int64))
+        _runs[name] = (np.array(chunks), h.hexdigest(), _state_digest(*sim.state()))
+        sim.close()
+    return _runs[name]
+
+
+@pytest.mark.parametrize("name", ["fp32", "bf16"])
+def test_ten_seconds_bit_identical_to_fp32_oracle(name):
+    fx = json.load(open(GOLDEN))
+    chunks, counts_sha, state_sha = _ten_seconds(name)
+    assert np.array_equal(chunks, np.array(fx[name]["chunk_counts"]))
+    assert counts_sha == fx[name]["counts_sha256"]
+    assert state_sha == fx[name]["state_sha256"]
+
+
+@pytest.mark.parametrize("name", ["fp32", "bf16"])
+def test_ten_seconds_rates_within_one_percent_of_fp64(name):
+    fx = json.load(open(GOLDEN))
+    tot = _ten_seconds(name)[0].sum(0)
+    tot64 = np.array(fx["fp64"]["chunk_counts"]).sum(0)
+    assert (tot64 > 0).all()
+    err = (tot - tot64) / tot64
+    path = os.environ.get("SGB_ACCURACY_OUT")
+    if path:
+        rec = json.load(open(path)) if os.path.exists(path) else {}
+        rec[f"{name}_rate_rel_error_10s"] = dict(zip(fx["populations"], err.tolist()))
+        with open(path, "w") as f:
+            json.dump(rec, f, indent=1)
+    bad = {p: e for p, e in zip(fx["populations"], err.tolist()) if abs(e) >= RATE_TOL}
+    assert not bad, f"{name}: populations off by >= 1 % over 10 s: {bad}"
+
+
+def _match_within_one(ids_a, off_a, ids_b, off_b):
     """Fraction of b's spikes that a has at the same cell within +-1 step."""
     n = len(off_b) - 1
     sets = [set(ids_a[off_a[s]:off_a[s + 1]].tolist()) for s in range(n)]
@@ -41,33 +111,27 @@ def _first_div(ids_a, off_a, ids_b, off_b):
     return len(off_a) - 1
 
 
-def test_bf16_and_fp32_against_fp64_oracle():
+def test_spike_timing_against_fp64_oracle():
     net = sg.scaffold(2, 1.0, 1)
-    d = oracle_py.describe(net)
-    nums = np.array([p["num"] for p in d["pops"]], float)
-    ref64 = oracle_py.Oracle(d, seed=1, mode=oracle_py.FP64)
-    c64, (i64, o64) = ref64.run(STEPS, raster_cap=1 << 24)
-    out = {"steps": STEPS, "populations": [p.name for p in net.populations]}
-    for name, wt in (("fp32", sg.WEIGHT_FP32), ("bf16", sg.WEIGHT_BF16)):
+    ref64 = oracle_py.Oracle(oracle_py.describe(net), seed=1, mode=oracle_py.FP64)
+    _, (i64, o64) = ref64.run(TIMING_STEPS, raster_cap=1 << 24)
+    out = {}
+    for name, wt in WEIGHTS.items():
         sim = sg.Simulation([net], [1], weight_type=wt, raster=True)
-        c, (ids, offs) = sim.loop_n_steps(STEPS, raster=True, raster_cap=1 << 24)
-        tot, tot64 = c.sum(0).astype(np.int64), c64.sum(0).astype(np.int64)
-        rate_err = (tot - tot64) / np.maximum(tot64, 1)
-        out[name] = {
-            "first_divergence_step": _first_div(ids, offs, i64, o64),
-            "matched_within_1_step": _match_within_one(ids, offs, i64, o64, net.counts()["neurons"]),
-            "rate_rel_error": rate_err.tolist(),
-            "rates_hz": (c.sum(0) / nums / (STEPS * 1e-4)).tolist(),
-        }
+        _, (ids, offs) = sim.loop_n_steps(TIMING_STEPS, raster=True, raster_cap=1 << 24)
+        out[name] = {"first_divergence_step": _first_div(ids, offs, i64, o64),
+                     "matched_within_1_step": _match_within_one(ids, offs, i64, o64)}
         sim.close()
-    out["fp64_rates_hz"] = (c64.sum(0) / nums / (STEPS * 1e-4)).tolist()
     path = os.environ.get("SGB_ACCURACY_OUT")
     if path:
+        rec = json.load(open(path)) if os.path.exists(path) else {}
+        rec["timing_first_4000_steps"] = out
         with open(path, "w") as f:
-            json.dump(out, f, indent=1)
-    for name in ("fp32", "bf16"):
-        # Populations with enough spikes for a rate to be meaningful.
-        r = np.abs(np.array(out[name]["rate_rel_error"]))[c64.sum(0) > 500]
-        assert (r < 0.05).all(), (name, out[name])
-        assert out[name]["matched_within_1_step"] > 0.5, (name, out[name])
-    assert out["fp32"]["first_divergence_step"] > 100
+            json.dump(rec, f, indent=1)
+    # FP32 tables follow the FP64 trajectory spike for spike for over a
+    # thousand steps and keep nearly every spike within one step after that;
+    # BF16 tables change individual threshold crossings within a few steps,
+    # and most spikes stay within one step.
+    assert out["fp32"]["first_divergence_step"] > 1000
+    assert out["fp32"]["matched_within_1_step"] > 0.999
+    assert out["bf16"]["matched_within_1_step"] > 0.7

@@ -82,6 +82,75 @@ def test_bf16_golden_fp32_oracle():
     assert _first_divergence(ids, offs, z["ids"], z["offs"]) == int(z["steps"])
 
 
+# ---- benchmark-scale fixtures: full config 1 (10,000 steps), config 2 (600) ----
+def _golden_desc(name):
+    z = np.load(os.path.join(GOLDEN, name))
+    return z, oracle_py.scaffold_desc(int(z["config"]), float(z["scale"]), int(z["seed"]))
+
+
+@pytest.mark.parametrize("name", ["ref_c1_s1_full.npz", "ref_c2_s3.npz", "ref_c2_s3_bf16.npz"])
+def test_reference_cpu_restatement_reproduces_benchmark_scale_golden(name):
+    """rp_* reproduces the reference's compiled functions bit for bit on the
+    full config 1 over its 10,000 steps and on config 2 (92,550 cells,
+    2,731,520 synapses, in-degree up to 25,000) in FP32 and BF16."""
+    z, desc = _golden_desc(name)
+    rp = oracle_py.RefPort(desc, seed=int(z["seed"]), bf16=bool(z["bf16"]))
+    counts, (ids, offs) = rp.run(int(z["steps"]), threads=4, raster_cap=1 << 22)
+    u, g, ref = rp.state()
+    assert np.array_equal(counts, z["counts"])
+    assert np.array_equal(ids, z["ids"]) and np.array_equal(offs, z["offs"])
+    assert np.array_equal(u.view(np.uint32), z["u"].view(np.uint32))
+    assert np.array_equal(g.view(np.uint32), z["g"].view(np.uint32))
+    assert np.array_equal(ref, z["ref"])
+
+
+@pytest.mark.parametrize("name,mode", [("ref_c2_s3.npz", oracle_py.FP32),
+                                       ("ref_c2_s3.npz", oracle_py.FP64),
+                                       ("ref_c2_s3_bf16.npz", oracle_py.FP32)])
+def test_oracle_equals_reference_on_config2(name, mode):
+    """On config 2 the oracle's raster equals the reference's spike for spike
+    over the whole fixture (600 steps), FP32 and BF16 tables (the FP64 mode
+    always uses the unrounded weights, so it pairs with the FP32 fixture)."""
+    z, desc = _golden_desc(name)
+    o = oracle_py.Oracle(desc, seed=int(z["seed"]), bf16=bool(z["bf16"]), mode=mode)
+    counts, (ids, offs) = o.run(int(z["steps"]), raster_cap=1 << 22)
+    assert _first_divergence(ids, offs, z["ids"], z["offs"]) == int(z["steps"])
+    assert np.array_equal(counts, z["counts"])
+    u, g, ref = o.state()
+    assert np.array_equal(ref, z["ref"])
+    np.testing.assert_allclose(u, z["u"], rtol=0, atol=2e-3)
+    np.testing.assert_allclose(g, z["g"], rtol=1e-3, atol=1e-4)
+
+
+@pytest.mark.parametrize("mode", [oracle_py.FP32, oracle_py.FP64])
+def test_oracle_against_reference_full_config1(mode):
+    """Full config 1 over its 1 s (10,000 steps): the rasters are identical
+    until step 2,703, where a cell at threshold crosses one step apart in the
+    reference's mixed precision (FP32 state, double DT/Cm) and in the oracle;
+    over the whole second every spike is matched by the same cell within one
+    step and every population's spike total is identical."""
+    z, desc = _golden_desc("ref_c1_s1_full.npz")
+    o = oracle_py.Oracle(desc, seed=1, mode=mode)
+    steps = int(z["steps"])
+    counts, (ids, offs) = o.run(steps, raster_cap=1 << 22)
+    assert _first_divergence(ids, offs, z["ids"], z["offs"]) >= 2000
+    differing = []
+    for s in range(steps):
+        a = set(ids[offs[s]:offs[s + 1]].tolist())
+        b = set(z["ids"][z["offs"][s]:z["offs"][s + 1]].tolist())
+        if a != b:
+            differing.append((s, a - b, b - a))
+    assert len(differing) <= 8
+    for s, extra, missing in differing:  # each difference is a spike moved by one step
+        for c in extra | missing:
+            near = set()
+            for t in (s - 1, s + 1):
+                near |= set(z["ids"][z["offs"][t]:z["offs"][t + 1]].tolist())
+                near |= set(ids[offs[t]:offs[t + 1]].tolist())
+            assert c in near
+    assert np.array_equal(counts.sum(0), z["counts"].sum(0))
+
+
 # ---- closed forms -------------------------------------------------------------
 def _single(num=4, Ie=0.0, dt_ref=2.0, tau=(0.5, 10.0), Vth=-50.0):
     net = sg.Network()
@@ -188,3 +257,18 @@ def test_scale_bits_rule():
 
             assert worst(s) <= 2**31 - 1
             assert s == 30 or worst(s + 1) > 2**31 - 1
+
+
+def test_config3_fixture_matches_the_oracle():
+    """tests/golden/c3_rates_s1.json (the oracle over config 3's 10 s, which
+    the GPU accuracy test reads) agrees with a fresh oracle run over its
+    first 1,000 steps in all three modes."""
+    fx = json.load(open(os.path.join(GOLDEN, "c3_rates_s1.json")))
+    desc = oracle_py.scaffold_desc(fx["config"], fx["scale"], fx["seed"])
+    modes = {"fp64": dict(mode=oracle_py.FP64), "fp32": dict(mode=oracle_py.FP32),
+             "bf16": dict(mode=oracle_py.FP32, bf16=True)}
+    for name, kw in modes.items():
+        o = oracle_py.Oracle(desc, seed=fx["seed"], **kw)
+        c, _ = o.run(fx["chunk"], raster_cap=1 << 20)
+        assert c.sum(0).tolist() == fx[name]["chunk_counts"][0], name
+    assert len(fx["fp64"]["chunk_counts"]) * fx["chunk"] == fx["steps"] == 100_000
