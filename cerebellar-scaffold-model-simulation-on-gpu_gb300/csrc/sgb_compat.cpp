@@ -201,6 +201,9 @@ void InitializeNetworkEnv(NetworkEnvironment* env, int T_print, int T_cpu_sim) {
   cfg.chunk_steps = T_cpu_sim;
   cfg.raster = 1;
   if (sgb_sim_create(&cfg, &env->net, &env->seed, 1, &env->sim)) die("InitializeNetworkEnv");
+  sgb_sim_info si;
+  if (sgb_sim_get_info(env->sim, &si)) die("InitializeNetworkEnv");
+  env->Host_sim_val[0].Host.neuron_num = (int)si.n_neurons;
   sgb_population_info pi;
   sgb_net_population_info(env->net, kDCN, &pi);
   const int32_t n_out = pi.num;

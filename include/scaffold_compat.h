@@ -11,7 +11,10 @@
  * in the directory named by the SGB_DAT_DIR environment variable (default:
  * the working directory, where the reference reads them), simulated with the
  * reference's 1-ms exchange step of 10 substeps of 0.1 ms.  Rasters are
- * written in the reference's text format to spike_output/.
+ * written in the reference's text format to spike_output/.  The reference's
+ * own main.cu also takes constants and enumerations from its
+ * GPUScaffoldSimulation.h: include/compat/GPUScaffoldSimulation.h provides
+ * them under that name.
  */
 #ifndef SCAFFOLD_COMPAT_H
 #define SCAFFOLD_COMPAT_H
@@ -22,7 +25,18 @@
 extern "C" {
 #endif
 
+/* The part of the reference's per-device record (cpu_sim_thread_val /
+ * Sim_cond_lif_exp, struct_enum_def.h:132-171) that its driver reads:
+ * Env.Host_sim_val[0].Host.neuron_num, the cells of the (one) device. */
+typedef struct sgb_compat_host {
+  int neuron_num;
+} sgb_compat_host;
+typedef struct sgb_compat_sim_val {
+  sgb_compat_host Host;
+} sgb_compat_sim_val;
+
 typedef struct NetworkEnvironment {
+  sgb_compat_sim_val Host_sim_val[1];  /* set by InitializeNetworkEnv */
   sgb_net* net;
   sgb_sim* sim;
   int num_of_neuron_types, num_of_connectivity_types, num_of_inputs;

@@ -24,6 +24,7 @@ int main(int argc, char** argv) {
   NetworkEnvironment Env;
   CreateNetworkEnv(&Env, 1, 7, 16, INPUT_STIM_NUM, 0);
   InitializeNetworkEnv(&Env, T_print, T_cpu_sim);
+  fprintf(stderr, "neuron_num = %d\n", Env.Host_sim_val[0].Host.neuron_num);
   float freq_list[INPUT_STIM_NUM];
   long dcn_spikes = 0;
   for (int trial = 0; trial < trials; trial++) {

@@ -94,6 +94,7 @@ def test_main_driver_through_compat_api(tmp_path):
     r = subprocess.run([exe, "1", "25", "50"], cwd=str(tmp_path), env=env, capture_output=True,
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
+    assert "neuron_num = 96737" in r.stderr  # Env.Host_sim_val[0].Host.neuron_num
     assert r.stdout.startswith("dcn_spikes ")
     out = tmp_path / "spike_output" / "spike_result_trial0.dat"
     lines = out.read_text().splitlines()
