@@ -179,6 +179,7 @@ struct StepArgs {
   uint32_t n_pad, n_words, n_segs, n_projs;
   uint32_t n_srcs;                // stimulus sources (all segments)
   uint32_t ring_slots, hist_rows;
+  uint32_t max_delay;             // longest synaptic delay, steps (ring_slots = max_delay + 2)
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
   uint32_t stdp_early;            // every plastic rule reads only earlier steps' spikes (Teacher)

@@ -421,7 +421,11 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     return set_error(SGB_ERR_UNSUPPORTED, "more than 2^27 cells (with padding) in one handle");
   s.n_words = s.n_pad / 32;
   s.n_cells = first_id;
-  s.ring_slots = (uint32_t)max_delay + 1;
+  // Ring slots t .. t + max_delay receive increments, plus one: the fused
+  // kernel's spike-ahead timeline reads slot t + 1 during step t and clears
+  // it during step t + 1, while pushes target slots up to t + 1 + max_delay.
+  s.max_delay = (uint32_t)max_delay;
+  s.ring_slots = (uint32_t)max_delay + 2;
   s.hist_rows = (uint32_t)max_delay;
   // A plastic synapse with delay d reads its pre cell's spikes d .. d +
   // window - 1 steps back, a teacher up to max_delay steps back.  Windows that
@@ -634,6 +638,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.n_projs = (uint32_t)s.projs.size();
   a.ring_slots = s.ring_slots;
   a.hist_rows = s.hist_rows;
+  a.max_delay = s.max_delay;
   a.n_upd_words = (uint32_t)upd_words.size();
   a.raster_cap = s.raster_cap;
   a.bf16 = s.bf16 ? 1 : 0;

@@ -529,14 +529,14 @@ __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit 
   return hits;
 }
 
-// The spike summary of steps t - d1, d1 = 0 .. ring_slots - 2 (the delay rows
+// The spike summary of steps t - d1, d1 = 0 .. max_delay - 1 (the delay rows
 // a pull of step t reads; a longer history kept for plasticity is not) into
 // shared memory as rows d1 of n_swords words, plus the zero word that
 // padding entries (row hist_rows) test; threads tid, tid + nthreads, ... with
 // four loads issued before their stores.  The caller synchronizes the block.
 __device__ __forceinline__ void stage_summary(const StepArgs& a, const StepIdx& ix, uint32_t* s_sum,
                                               uint32_t tid, uint32_t nthreads) {
-  const uint32_t R = a.hist_rows + 1u, n = (a.ring_slots - 1u) * a.n_swords;
+  const uint32_t R = a.hist_rows + 1u, n = a.max_delay * a.n_swords;
   for (uint32_t j0 = tid; j0 < n; j0 += 4u * nthreads) {
     uint32_t v[4];
 #pragma unroll
@@ -1579,7 +1579,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     // unread, so a launch ends in the same state as with the other timeline.
     // The ring slot a LIF word consumes next is staged in shared memory by
     // asynchronous 16-byte copies at L2 (cp.async.cg: never a stale L1 line),
-    // so no registers are held for it across the pushes and the barrier.
+    // so no registers are held for it across the pushes and the barrier.  The
+    // slot is cleared at the start of the step that consumes it: with
+    // max_delay + 2 ring slots no push of that step targets it, and the
+    // clears' acknowledgements return during the update, not at the
+    // barrier's release.
     __shared__ __align__(16) int2 s_acc[kPersistBlock];
     int2* ring2 = reinterpret_cast<int2*>(a.ring);
     const bool rd = has && lif && valid;
@@ -1592,13 +1596,6 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    // After the warp's copies landed: the fetched entries, cleared in the ring.
-    auto clear_slot = [&](uint32_t roff) {
-      asm volatile("cp.async.wait_all;" ::: "memory");
-      __syncwarp();
-      const int2 v = s_acc[threadIdx.x];
-      if (rd && (v.x | v.y)) __stcg(ring2 + (roff + i), make_int2(0, 0));
-    };
     bool in_next = false;  // input spike of step t + 1, drawn a step ahead
     if (n_steps) {
       if (fetch) fetch_slot(ix.roff);
@@ -1609,11 +1606,18 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       off = nit = 0;
       if (has) publish(valid && (lif ? st.x > segs[seg].Vth : next_in), ix, 0u, 0u);
       deliver(0u, ix.slot, ix.slot, kNoRow);
-      if (fetch) clear_slot(ix.roff);
       grid_arrive(a, target);
       aborted = !grid_wait(a, target, s_poller);
     }
     for (uint32_t s = 0; s < n_steps && !aborted; ++s) {
+      // Ring slot t, fetched during the previous step: consumed and cleared.
+      int2 acc = make_int2(0, 0);
+      if (fetch) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncwarp();
+        acc = s_acc[threadIdx.x];
+        if (rd && (acc.x | acc.y)) __stcg(ring2 + (ix.roff + i), make_int2(0, 0));
+      }
       StepIdx nx = ix;
       nx.t = ix.t + 1ull;
       nx.rel = s + 1u;
@@ -1632,10 +1636,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         bool fired = false;
         if (lif) {
           const LifK k = lif_k(segs[seg]);
-          if (rd) lif_update<1>(k, 1, st, s_acc[threadIdx.x]);
+          if (rd) lif_update<1>(k, 1, st, acc);
           fired = valid && st.x > k.Vth;
           // Ring slot t + 1: complete since the last grid barrier; its copy
-          // lands while the block pushes.
+          // lands while the block pushes and waits at the barrier.
           if (more) fetch_slot(ix.roff);
         } else {
           fired = in_next;
@@ -1644,7 +1648,6 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       }
       const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
       deliver(par, ix.slot, shard_slot, sh_from);
-      if (fetch && more) clear_slot(ix.roff);
       grid_arrive(a, target);
       if (stim && s + 2u < n_steps)
         in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
