@@ -39,7 +39,7 @@ void sgb_config_init(sgb_config* cfg) {
 
 const char* sgb_last_error(void) { return last_error(); }
 
-int32_t sgb_abi_version(void) { return 2; }
+int32_t sgb_abi_version(void) { return 3; }
 
 int sgb_net_create(sgb_net** out) {
   if (!out) return set_error(SGB_ERR_ARG, "out is NULL");
@@ -319,6 +319,10 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
                           : SGB_KERNEL_GRAPH;
   info->push_smem_bytes = info->step_kernel == SGB_KERNEL_FUSED ? (int32_t)s.args.row_smem : 0;
   info->shard_cells = info->step_kernel == SGB_KERNEL_FUSED ? s.n_shard_cells : 0;
+  info->item_width = 1 << s.args.item_log2;
+  info->deliver_blocks = s.deliver_blocks;
+  info->pull_summary = (int32_t)s.args.pull_sum;
+  info->spike_ahead = info->step_kernel == SGB_KERNEL_FUSED && s.cfg.substeps == 1 && s.args.ahead;
   info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;
   info->weight_type = s.cfg.weight_type;

@@ -180,13 +180,17 @@ struct StepArgs {
   uint32_t n_srcs;                // stimulus sources (all segments)
   uint32_t ring_slots, hist_rows;
   uint32_t max_delay;             // longest synaptic delay, steps (ring_slots = max_delay + 2)
+  uint32_t item_log2;             // fused persistent kernel: push items of 2^item_log2 synapses
+  uint32_t ahead;                 // fused persistent kernel: spike-ahead timeline (one substep)
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
   uint32_t stdp_early;            // every plastic rule reads only earlier steps' spikes (Teacher)
   uint32_t seg_smem;              // general persistent kernel: segment descriptors in shared memory
   uint32_t bar_extra;             // tests only: barrier arrivals that never come
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
-  uint32_t pull_sum;              // 1: k_pull stages the summary in shared memory
+  uint32_t pull_sum;              // dense pulls: 0 every entry loads its history word; 1 entries
+                                  // settle on a staged spike summary; 2 as 1, the per-step
+                                  // kernel also staging its entry stream (k_pull_async)
   uint32_t any_push;
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer
@@ -224,6 +228,7 @@ cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t pull_setup();
 int pull_blocks_per_sm(const StepArgs& a);
 size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summary rows
+size_t pull_async_smem_bytes(const StepArgs& a);  // k_pull_async: summary + entry buffers
 size_t seg_smem_bytes(const StepArgs& a);  // shared memory of the segment descriptors
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
 int persistent_kernel_kind(const StepArgs& a, int blocks);

@@ -645,6 +645,16 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.substeps = cfg.substeps;
   a.bar_extra = (uint32_t)cfg.barrier_test_extra;
   s.deliver_blocks = 2 * s.sm_count;
+  a.item_log2 = 6;  // push items of 64 synapses (the autotuner may pick 32 or 128)
+  a.ahead = 1;      // spike-ahead timeline of the fused kernel (one-substep steps)
+  // Dense pulls settle entries on the staged summary where it fits, and the
+  // per-step pull kernel also stages its entry stream where that fits too.
+  {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device);
+    if (a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin) a.pull_sum = 2u;
+  }
+  s.pull_sum_fits = a.pull_sum;
   // The cell state is read and rewritten every step; where the device lets
   // this context set L2 aside for persisting accesses, the state window
   // stays in L2 across steps while ring slots, tables and history stream
@@ -1139,10 +1149,35 @@ static std::string tune_signature(const Sim& s) {
   return buf;
 }
 
+// Launch shapes the autotuner picks beside the modes and the driver.
+struct TuneShape {
+  int32_t item_log2;     // fused kernel: push items of 2^item_log2 synapses
+  int32_t deliver_mult;  // per-step driver: delivery blocks per SM
+  int32_t pull_sum;      // dense pulls: 0 no summary, 1 staged summary, 2 also staged entries
+  int32_t ahead;         // fused kernel: 1 spike-ahead timeline, 0 spikes in their own step
+};
+
+static TuneShape current_shape(const Sim& s) {
+  return {(int32_t)s.args.item_log2, std::max(1, s.deliver_blocks / std::max(1, s.sm_count)),
+          (int32_t)s.args.pull_sum, (int32_t)s.args.ahead};
+}
+
+// Applies a shape (kept within what the handle supports); captured graphs
+// hold the old kernel arguments and are dropped.
+static void apply_shape(Sim& s, const TuneShape& t) {
+  s.args.item_log2 = (uint32_t)std::min(7, std::max(5, t.item_log2));
+  s.deliver_blocks = std::min(8, std::max(1, t.deliver_mult)) * s.sm_count;
+  s.args.pull_sum = (uint32_t)std::min<int32_t>(std::max(0, t.pull_sum), (int32_t)s.pull_sum_fits);
+  s.args.ahead = t.ahead ? 1u : 0u;
+  for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
+  s.graphs.clear();
+}
+
 // Reads the cached decision for `sig` from a JSON-lines file:
-// {"signature": "<hex>", "exec_mode": m, "modes": [a, b, ...], "us_per_step": x}
+// {"signature": "<hex>", "exec_mode": m, "modes": [a, b, ...],
+//  "shape": [item_log2, deliver_mult, pull_sum], "us_per_step": x}
 static bool tune_cache_read(const char* path, const std::string& sig, int32_t* exec_mode,
-                            std::vector<int32_t>& modes) {
+                            std::vector<int32_t>& modes, TuneShape* shape) {
   FILE* f = path ? fopen(path, "rb") : nullptr;
   if (!f) return false;
   char line[1 << 16];
@@ -1161,6 +1196,12 @@ static bool tune_cache_read(const char* path, const std::string& sig, int32_t* e
       modes.push_back((int32_t)v);
       p = q;
     }
+    const char* sh = strstr(line, "\"shape\": [");
+    if (sh && shape) {
+      int32_t v[4] = {6, 2, 1, 1};
+      if (sscanf(sh + 10, "%d , %d , %d , %d", &v[0], &v[1], &v[2], &v[3]) >= 3)
+        *shape = {v[0], v[1], v[2], v[3]};
+    }
     found = true;
   }
   fclose(f);
@@ -1168,13 +1209,15 @@ static bool tune_cache_read(const char* path, const std::string& sig, int32_t* e
 }
 
 static void tune_cache_write(const char* path, const std::string& sig, int32_t exec_mode,
-                             const std::vector<int32_t>& modes, double us_per_step) {
+                             const std::vector<int32_t>& modes, const TuneShape& shape,
+                             double us_per_step) {
   if (!path) return;
   FILE* f = fopen(path, "ab");
   if (!f) return;
   fprintf(f, "{\"signature\": \"%s\", \"exec_mode\": %d, \"modes\": [", sig.c_str(), exec_mode);
   for (size_t i = 0; i < modes.size(); ++i) fprintf(f, "%s%d", i ? ", " : "", modes[i]);
-  fprintf(f, "], \"us_per_step\": %.4f}\n", us_per_step);
+  fprintf(f, "], \"shape\": [%d, %d, %d, %d], \"us_per_step\": %.4f}\n", shape.item_log2,
+          shape.deliver_mult, shape.pull_sum, shape.ahead, us_per_step);
   fclose(f);
 }
 
@@ -1192,8 +1235,11 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   const std::string sig = tune_signature(s);
   std::vector<int32_t> modes;
   int32_t exec_mode = s.cfg.exec_mode;
-  if (tune_cache_read(cache_path, sig, &exec_mode, modes) && modes.size() == s.projs.size()) {
+  TuneShape shape = current_shape(s);
+  if (tune_cache_read(cache_path, sig, &exec_mode, modes, &shape) &&
+      modes.size() == s.projs.size()) {
     s.cfg.exec_mode = exec_mode;
+    apply_shape(s, shape);
     return apply_modes(s, modes);
   }
   // Snapshot of the device state a run changes.
@@ -1273,8 +1319,35 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   if (us_other < best * 0.98) best = us_other; else s.cfg.exec_mode = mine;
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
+  // Launch shapes for the chosen driver and modes, one dimension at a time:
+  // the fused kernel's push-item width, the per-step delivery grid, and
+  // whether dense pulls settle entries on a staged spike summary.
+  {
+    TuneShape cur = current_shape(s);
+    std::vector<TuneShape> cands;
+    const bool persistent = s.cfg.exec_mode == SGB_EXEC_PERSISTENT;
+    if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_FUSED &&
+        s.cfg.substeps == 1) {
+      for (int32_t w : {5, 7}) cands.push_back({w, cur.deliver_mult, cur.pull_sum, 1});
+      cands.push_back({6, cur.deliver_mult, cur.pull_sum, 0});  // the other timeline
+    }
+    if (!persistent)
+      for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead});
+    // Pull variants below the default: without staged entries, without summary.
+    for (int32_t ps = (int32_t)s.pull_sum_fits - 1; s.args.n_pull_units && ps >= 0; --ps)
+      cands.push_back({-1 - ps, -1, -1, -1});
+    for (TuneShape c : cands) {
+      if (c.item_log2 < 0) c = {cur.item_log2, cur.deliver_mult, -1 - c.item_log2, cur.ahead};
+      apply_shape(s, c);
+      double us = 0;
+      if ((rc = measure(&us))) return fail(rc);
+      if (us < best * 0.98) { best = us; cur = c; }
+    }
+    apply_shape(s, cur);
+    shape = cur;
+  }
   if (save(true)) return fail(set_error(SGB_ERR_CUDA, "autotune restore failed"));
-  tune_cache_write(cache_path, sig, s.cfg.exec_mode, modes, best);
+  tune_cache_write(cache_path, sig, s.cfg.exec_mode, modes, shape, best);
   return fail(SGB_OK);
 }
 

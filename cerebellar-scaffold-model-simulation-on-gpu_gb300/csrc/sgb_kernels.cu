@@ -16,7 +16,9 @@
 //            (the reference's pull, Simulation_header.cu:83-139, with the delay
 //            applied on read as at GPUScaffoldSimulation.cu:735).
 // Two drivers run these phases: per-step kernels (replayed from a CUDA graph;
-// kernel boundaries order the phases) and one persistent cooperative kernel
+// kernel boundaries order the phases; the dense pull streams its entries
+// through shared memory with asynchronous copies, two half units in flight
+// per warp, where they fit) and one persistent cooperative kernel
 // per chunk of steps (a bounded grid barrier orders them).  The persistent
 // kernel comes in three forms: fused (every word resident in one warp, every
 // projection event-driven: update and push share one phase, one barrier a
@@ -31,6 +33,8 @@
 // ring holds int32 fixed-point sums, so push and pull delivery, any launch
 // order and any number of instances give bit-identical conductances.
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "sgb_device.h"
 #include "sgb_philox.h"
@@ -733,6 +737,94 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
   if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
 }
 
+// Dense pull with the entry stream staged in shared memory (per-step driver;
+// one 1,024-thread block per SM).  A warp takes half units (512 entries, 2 KB)
+// gw, gw + nw, ... and keeps two of them in flight: each lane copies 16-byte
+// chunks of a half unit into the warp's shared-memory buffer with cp.async.cg
+// (at L2, no registers held), and while one buffer is settled the other one
+// loads.  Settling reads the entries from shared memory: the summary test
+// (s_sum, staged as in k_pull) passes few of them, the passing ones load their
+// history word (four at a time) and the hits add their weight into the ring.
+// Shared memory: the staged summary, then 2 x 2 KB per warp.
+constexpr uint32_t kHalfUnit = kPullUnit / 2;
+constexpr size_t kPullBufBytes = (size_t)(kPullBlock / 32) * 2 * kHalfUnit * 4;  // 128 KiB
+template <bool BF16>
+__global__ void __launch_bounds__(kPullBlock, 1) k_pull_async(StepArgs a) {
+  constexpr uint32_t E = kHalfUnit / 32;  // entries per lane per half unit
+  constexpr uint32_t W = 4;               // history words loaded per trip
+  extern __shared__ __align__(16) uint32_t s_sum[];  // [H][n_swords] + 1, then the buffers
+  const size_t sum_words = ((size_t)a.hist_rows * a.n_swords + 1 + 3) & ~(size_t)3;
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  uint32_t* buf = s_sum + sum_words + (size_t)wib * 2u * kHalfUnit;
+  const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
+  const uint32_t n = 2u * a.n_pull_units;  // half units
+  const StepIdx ix = step_of(a);
+  const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+  // Copies half unit v into buffer b (lane: chunks lane, lane + 32, ...).
+  auto issue = [&](uint32_t v, uint32_t b) {
+    if (v < n) {
+      const PullUnit un = a.pull_units[v >> 1];
+      const uint32_t* src = a.projs[un.proj].ell_syn + un.o0 + (v & 1u) * kHalfUnit;
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(buf + b * kHalfUnit);
+#pragma unroll
+      for (uint32_t c = 0; c < kHalfUnit / 4 / 32; ++c) {
+        const uint32_t k = c * 32u + lane;  // 16-byte chunk index
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + k * 16u),
+                     "l"(src + k * 4u) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  issue(gw, 0u);
+  issue(gw + nw, 1u);
+  stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
+  __syncthreads();
+  const uint32_t* hb = hist_base(a, ix.hrow);
+  uint32_t hits = 0;
+  uint32_t b = 0;
+  for (uint32_t v = gw; v < n; v += nw, b ^= 1u) {
+    // The older of the two groups in flight is this buffer's.
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    const uint32_t* e = buf + b * kHalfUnit;
+    const PullUnit un = a.pull_units[v >> 1];
+    const ProjDev& P = a.projs[un.proj];
+    const uint32_t o0 = un.o0 + (v & 1u) * kHalfUnit;
+    uint32_t need = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < E; ++k) {
+      const uint32_t ek = e[k * 32u + lane];
+      const uint32_t sw = s_sum[ek >> 10];
+      need |= (__funnelshift_r(sw, sw, ek >> 5) & 1u) << k;
+    }
+    while (need) {
+      uint32_t ks[W], ev[W], hw[W];
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) {
+        ks[j] = need ? __ffs(need) - 1u : E;
+        need &= need - 1u;
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) ev[j] = ks[j] < E ? e[ks[j] * 32u + lane] : 0u;
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) hw[j] = ks[j] < E ? __ldg(hb + (ev[j] >> 5)) : 0u;
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) {
+        if (ks[j] < E && ((hw[j] >> (ev[j] & 31u)) & 1u)) {
+          ++hits;
+          pull_hit<BF16>(a, P, o0 + ks[j] * 32u + lane, slot1);
+        }
+      }
+    }
+    __syncwarp();  // every lane is done with this buffer
+    issue(v + 2u * nw, b);
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  hits = __reduce_add_sync(kFull, hits);
+  if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
+}
+
 // STDP of the plastic projections, step t (SynapticPlasticity.cu:40-120), run
 // after the cells of step t updated and before the dense pull that delivers
 // into slot t + 1, so that delivery uses the new values -- in the reference
@@ -1250,10 +1342,10 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_resident(StepAr
 // order, each row whole or not at all; rows past the capacity stay in global
 // memory), so a step's pushes read no global memory.
 constexpr uint32_t kBlockItems = 2048;  // push items per block and step (16 KiB)
-// Own rows are cut into items of kFusedChunk synapses (2 per lane): a block
-// usually pushes one or two spikes' rows a step, and smaller items spread
-// their scattered reductions over more of its warps.
-constexpr uint32_t kFusedChunk = 64;
+// Own rows are cut into items of 2^a.item_log2 synapses (32, 64 or 128; 64 =
+// two per lane unless the autotuner picked another width): a block usually
+// pushes one or two spikes' rows a step, and smaller items spread their
+// scattered reductions over more of its warps.
 
 // An item of the fused kernel: (first synapse, length << 23 | flags); flag 1:
 // the synapses are in the block's shared-memory rows, flag 2: a shard of the
@@ -1266,7 +1358,8 @@ __device__ __forceinline__ uint32_t push_any(const StepArgs& a, const uint2* row
 }
 
 // AHEAD: the spike-ahead timeline of one-substep steps (see the loop below).
-template <bool BF16, bool AHEAD>
+// ILOG: push items of 2^ILOG synapses.
+template <bool BF16, bool AHEAD, uint32_t ILOG>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs a,
                                                                        uint32_t n_steps) {
   __shared__ uint2 s_items[kBlockItems];
@@ -1415,6 +1508,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   // memory and its length, with bit 31 set when it is in shared memory.
   const uint32_t qb = sb != kNoRow ? sb : r0;
   const uint32_t rl = len | (sb != kNoRow ? 0x80000000u : 0u);
+  constexpr uint32_t clog = ILOG, chunk = 1u << ILOG;  // push-item width
   unsigned long long target = 0;
   uint32_t walked = 0;
   bool aborted = false;
@@ -1425,7 +1519,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   uint32_t off = 0, nit = 0;
   // Spike bookkeeping of this warp's word for the spikes of step px.t (chunk
   // row `rel`): history and summary bits, per-segment count, events, raster
-  // entries, and the spiking cells' rows cut into kFusedChunk-synapse items
+  // entries, and the spiking cells' rows cut into chunk-synapse items
   // in the block's list of parity `par`.
   auto publish = [&](bool fired, const StepIdx& px, uint32_t rel, uint32_t par) {
     off = 0;
@@ -1436,7 +1530,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     const uint32_t n = __popc(ballot);
     const uint32_t rank = __popc(ballot & ((1u << lane) - 1u));
     const uint32_t ev = __reduce_add_sync(kFull, fired ? s_od[threadIdx.x] : 0u);
-    nit = fired ? ((rl & 0x7FFFFFFFu) + kFusedChunk - 1) / kFusedChunk : 0u;
+    nit = fired ? ((rl & 0x7FFFFFFFu) + chunk - 1) >> clog : 0u;
     uint32_t incl = nit;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -1453,8 +1547,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     }
     off = __shfl_sync(kFull, off, 0) + incl - nit;
     for (uint32_t k = 0; k < nit && off + k < kBlockItems; ++k) {
-      const uint32_t q = k * kFusedChunk;
-      s_items[off + k] = make_uint2(qb + q, (min(kFusedChunk, (rl & 0x7FFFFFFFu) - q) << 23) |
+      const uint32_t q = k << clog;
+      s_items[off + k] = make_uint2(qb + q, (min(chunk, (rl & 0x7FFFFFFFu) - q) << 23) |
                                                 (rl >> 31));
     }
     if (a.raster_cap) {
@@ -1468,18 +1562,18 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     }
   };
   // A spiking shard (its cell's bit set in the history word sh_w) becomes
-  // kFusedChunk-synapse items of parity par; returns the first item past the
+  // chunk-synapse items of parity par; returns the first item past the
   // list's capacity, which this thread's warp pushes itself (kNoRow: none).
   auto shard_items = [&](bool ck, uint32_t sh_w, uint32_t par) -> uint32_t {
     uint32_t from = kNoRow;
     if (ck) {
       const uint4 h = s_sh[threadIdx.x];
       if ((sh_w >> (h.x & 31u)) & 1u) {
-        const uint32_t sl = h.z >> 23, ni = (sl + kFusedChunk - 1) / kFusedChunk;
+        const uint32_t sl = h.z >> 23, ni = (sl + chunk - 1) >> clog;
         const uint32_t o = atomicAdd(&s_n[par], ni);
         for (uint32_t k = 0; k < ni && o + k < kBlockItems; ++k)
-          s_items[o + k] = make_uint2(h.y + k * kFusedChunk,
-                                      (min(kFusedChunk, sl - k * kFusedChunk) << 23) | (h.z & 3u));
+          s_items[o + k] = make_uint2(h.y + (k << clog),
+                                      (min(chunk, sl - (k << clog)) << 23) | (h.z & 3u));
         if (o + ni > kBlockItems) from = o < kBlockItems ? kBlockItems - o : 0u;
       }
     }
@@ -1502,8 +1596,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       const uint32_t o = __shfl_sync(kFull, off, src), c = __shfl_sync(kFull, nit, src);
       const uint32_t b0 = __shfl_sync(kFull, qb, src), bl = __shfl_sync(kFull, rl, src);
       for (uint32_t k = o < kBlockItems ? kBlockItems - o : 0; k < c; ++k) {
-        const uint32_t q = k * kFusedChunk;
-        const uint2 it = make_uint2(b0 + q, (min(kFusedChunk, (bl & 0x7FFFFFFFu) - q) << 23) | (bl >> 31));
+        const uint32_t q = k << clog;
+        const uint2 it = make_uint2(b0 + q, (min(chunk, (bl & 0x7FFFFFFFu) - q) << 23) | (bl >> 31));
         walked += push_any<BF16>(a, s_rows, it, own, shard);
       }
     }
@@ -1514,9 +1608,9 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         sp &= sp - 1;
         const uint4 h = s_sh[wib * 32u + src];
         const uint32_t sl = h.z >> 23;
-        for (uint32_t q = __shfl_sync(kFull, sh_from, src) * kFusedChunk; q < sl; q += kFusedChunk)
+        for (uint32_t q = __shfl_sync(kFull, sh_from, src) << clog; q < sl; q += chunk)
           walked += push_any<BF16>(
-              a, s_rows, make_uint2(h.y + q, (min(kFusedChunk, sl - q) << 23) | (h.z & 3u)), own,
+              a, s_rows, make_uint2(h.y + q, (min(chunk, sl - q) << 23) | (h.z & 3u)), own,
               shard);
       }
     }
@@ -1638,9 +1732,6 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
           const LifK k = lif_k(segs[seg]);
           if (rd) lif_update<1>(k, 1, st, acc);
           fired = valid && st.x > k.Vth;
-          // Ring slot t + 1: complete since the last grid barrier; its copy
-          // lands while the block pushes and waits at the barrier.
-          if (more) fetch_slot(ix.roff);
         } else {
           fired = in_next;
         }
@@ -1649,6 +1740,11 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
       deliver(par, ix.slot, shard_slot, sh_from);
       grid_arrive(a, target);
+      // Ring slot t + 1 has been complete since the previous grid barrier and
+      // nothing writes it before this warp clears it next step, so its copy is
+      // issued after the arrival (the release does not wait for it) and lands
+      // while the block waits at the barrier.
+      if (fetch && more) fetch_slot(ix.roff);
       if (stim && s + 2u < n_steps)
         in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
       if (!grid_wait(a, target, s_poller)) {
@@ -1695,8 +1791,19 @@ size_t seg_smem_bytes(const StepArgs& a) { return seg_smem_bytes_dev(a); }
 
 static size_t pull_smem_bytes(const StepArgs& a) { return a.pull_sum ? pull_sum_bytes(a) : 0; }
 
+// k_pull_async: the staged summary (rounded to 16 bytes) and the warps' buffers.
+size_t pull_async_smem_bytes(const StepArgs& a) {
+  return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + kPullBufBytes;
+}
+
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
   if (!a.n_pull_units) return cudaSuccess;
+  if (a.pull_sum == 2u) {
+    const size_t smem = pull_async_smem_bytes(a);
+    if (a.bf16) k_pull_async<true><<<blocks, kPullBlock, smem, s>>>(a);
+    else k_pull_async<false><<<blocks, kPullBlock, smem, s>>>(a);
+    return cudaGetLastError();
+  }
   const size_t smem = pull_smem_bytes(a);
   if (a.bf16) {
     if (a.pull_sum) k_pull<true, true><<<blocks, kPullBlock, smem, s>>>(a);
@@ -1732,6 +1839,11 @@ cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s) {
 cudaError_t pull_setup() {
   const int mx = (int)kPullSumMax;
   cudaError_t e;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if ((e = cudaFuncSetAttribute(k_pull_async<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
+  if ((e = cudaFuncSetAttribute(k_pull_async<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
@@ -1758,6 +1870,30 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// The fused kernel's forms: [BF16][timeline: 0 as read, 1..3 spike-ahead with
+// push items of 32, 64, 128 synapses].
+static const void* const kFusedKernels[] = {
+    (const void*)k_persistent_fused<false, false, 6>, (const void*)k_persistent_fused<false, true, 5>,
+    (const void*)k_persistent_fused<false, true, 6>, (const void*)k_persistent_fused<false, true, 7>,
+    (const void*)k_persistent_fused<true, false, 6>, (const void*)k_persistent_fused<true, true, 5>,
+    (const void*)k_persistent_fused<true, true, 6>, (const void*)k_persistent_fused<true, true, 7>};
+
+static const void* fused_kernel(const StepArgs& a) {
+  const uint32_t form =
+      a.substeps == 1 && a.ahead ? std::min(7u, std::max(5u, a.item_log2)) - 4u : 0u;
+  return kFusedKernels[(a.bf16 ? 4u : 0u) + form];
+}
+
+static int fused_blocks_per_sm() {
+  int n = 1 << 20;
+  for (const void* fn : kFusedKernels) {
+    int f = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, fn, kPersistBlock, 0);
+    n = f < n ? f : n;
+  }
+  return n;
+}
+
 int persistent_blocks_per_sm(bool bf16) {
   int n = 0, m = 0;
   int f = 0;
@@ -1766,18 +1902,12 @@ int persistent_blocks_per_sm(bool bf16) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<true, true>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<true, true>, kPersistBlock, 0);
-    int g = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g, k_persistent_fused<true, false>, kPersistBlock, 0);
-    f = f < g ? f : g;
+    f = fused_blocks_per_sm();
   } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<false, true>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_persistent_fused<false, true>, kPersistBlock, 0);
-    int g = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g, k_persistent_fused<false, false>, kPersistBlock, 0);
-    f = f < g ? f : g;
+    f = fused_blocks_per_sm();
   }
   n = n < m ? n : m;
   n = n < o ? n : o;
@@ -1803,11 +1933,7 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
   const int kind = persistent_kernel_kind(a, blocks);
   const bool resident = kind != SGB_KERNEL_GENERAL;
   const bool fused = kind == SGB_KERNEL_FUSED;
-  const bool ahead = a.substeps == 1;
-  const void* fn = fused      ? (a.bf16 ? (ahead ? (const void*)k_persistent_fused<true, true>
-                                                 : (const void*)k_persistent_fused<true, false>)
-                                        : (ahead ? (const void*)k_persistent_fused<false, true>
-                                                 : (const void*)k_persistent_fused<false, false>))
+  const void* fn = fused      ? fused_kernel(a)
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
                                         : (const void*)k_persistent_resident<false>)
                    : general_one_barrier(a)
@@ -1825,11 +1951,7 @@ uint32_t fused_row_smem_max() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   size_t st = 0;
-  const void* fns[] = {(const void*)k_persistent_fused<false, false>,
-                       (const void*)k_persistent_fused<false, true>,
-                       (const void*)k_persistent_fused<true, false>,
-                       (const void*)k_persistent_fused<true, true>};
-  for (const void* fn : fns) {
+  for (const void* fn : kFusedKernels) {
     cudaFuncAttributes fa{};
     cudaFuncGetAttributes(&fa, fn);
     st = fa.sharedSizeBytes > st ? fa.sharedSizeBytes : st;
@@ -1838,11 +1960,7 @@ uint32_t fused_row_smem_max() {
 }
 
 cudaError_t set_fused_row_smem(uint32_t bytes) {
-  const void* fns[] = {(const void*)k_persistent_fused<false, false>,
-                       (const void*)k_persistent_fused<false, true>,
-                       (const void*)k_persistent_fused<true, false>,
-                       (const void*)k_persistent_fused<true, true>};
-  for (const void* fn : fns) {
+  for (const void* fn : kFusedKernels) {
     const cudaError_t e =
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e) return e;

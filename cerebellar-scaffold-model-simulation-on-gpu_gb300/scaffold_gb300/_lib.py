@@ -86,7 +86,9 @@ class SimInfo(C.Structure):
                 ("dt_ms", C.c_double), ("events", C.c_int64), ("delivered", C.c_int64),
                 ("step_kernel", C.c_int32), ("push_smem_bytes", C.c_int32), ("pulled", C.c_int64),
                 ("pull_entries", C.c_int64), ("l2_persist_bytes", C.c_int64),
-                ("shard_cells", C.c_int64)]
+                ("shard_cells", C.c_int64), ("item_width", C.c_int32),
+                ("deliver_blocks", C.c_int32), ("pull_summary", C.c_int32),
+                ("spike_ahead", C.c_int32)]
 
 
 P = C.POINTER

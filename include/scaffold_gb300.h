@@ -170,6 +170,13 @@ typedef struct sgb_sim_info {
   int64_t pull_entries;  /* dense-table entries streamed per step (0 without dense projections) */
   int64_t l2_persist_bytes; /* L2 set aside for the persisting state window (0: none)   */
   int64_t shard_cells;   /* SGB_KERNEL_FUSED: cells whose delay >= 2 synapses other blocks push */
+  /* Launch shapes (defaults, or the autotuner's choice): */
+  int32_t item_width;     /* SGB_KERNEL_FUSED: synapses per push item (32, 64 or 128)      */
+  int32_t deliver_blocks; /* per-step driver: blocks of the delivery kernel               */
+  int32_t pull_summary;   /* dense pulls: 0 every entry reads its history word; 1 entries   */
+                          /* settle on a staged spike summary; 2 as 1, the per-step pull  */
+                          /* also staging its entry stream in shared memory               */
+  int32_t spike_ahead;    /* SGB_KERNEL_FUSED: 1 the spike-ahead timeline (one substep)   */
 } sgb_sim_info;
 
 /* Step kernels (sgb_sim_info.step_kernel). */

@@ -35,7 +35,7 @@ def test_config_defaults_and_errors():
     L.lib().sgb_config_init(C.byref(cfg))
     assert (cfg.dt_ms, cfg.substeps, cfg.chunk_steps, cfg.weight_type, cfg.exec_mode) == (
         0.1, 1, 1000, sg.WEIGHT_FP32, sg.EXEC_GRAPH)
-    assert L.lib().sgb_abi_version() == 2
+    assert L.lib().sgb_abi_version() == 3
     rc = L.lib().sgb_net_create(None)
     assert rc == -1 and b"NULL" in L.lib().sgb_last_error()
     assert L.lib().sgb_sim_run(None, 10, None, None, 0, None) == -1

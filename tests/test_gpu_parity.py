@@ -339,3 +339,48 @@ def test_general_kernel_block_item_overflow(delay):
     assert counts[:, 0].sum() == n_src * steps and counts[:, 1].sum() > 0
     assert sim.info().delivered == exp[6]
     sim.close()
+
+
+@pytest.mark.parametrize("exec_mode,prop,shape", [
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [5, 2, 1, 1]),  # fused, spike-ahead, 32-synapse items
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [7, 2, 1, 1]),  # fused, spike-ahead, 128-synapse items
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [6, 2, 1, 0]),  # fused, spikes in their own step
+    (sg.EXEC_GRAPH, None, [6, 1, 0, 1]),              # per-step kernels: 1 delivery block per SM, no summary
+    (sg.EXEC_GRAPH, None, [6, 4, 1, 1]),              # k_pull with registers (summary, entries not staged)
+    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 2, 1]),       # k_pull_async: entry stream staged in shared memory
+    (sg.EXEC_PERSISTENT, sg.PROP_ELL, [6, 4, 0, 1]),  # resident kernel, pulls without the summary
+])
+def test_cached_launch_shapes_bit_exact(tmp_path, exec_mode, prop, shape):
+    """The autotuner's decisions (driver, propagation modes, launch shapes)
+    are cached as one JSON line and applied as they are by a later handle; every
+    launch shape it may pick gives the same bit-exact run.  The line is written
+    by a first tuning run and then edited to the combination under test."""
+    import json
+
+    net = sg.scaffold(2, 1.0, 3)
+    cache = str(tmp_path / "tune.jsonl")
+    first = sg.Simulation([net], [3], chunk_steps=100)
+    first.autotune(20, cache)
+    first.close()
+    line = json.loads(open(cache).read().splitlines()[0])
+    n = len(net.projections)
+    line["exec_mode"] = exec_mode
+    line["modes"] = [prop if prop is not None else (sg.PROP_ELL if j % 2 else sg.PROP_CSR)
+                     for j in range(n)]
+    line["shape"] = shape
+    with open(cache, "w") as f:
+        f.write(json.dumps(line) + "\n")
+    sim = sg.Simulation([net], [3], raster=True, chunk_steps=100)
+    sim.autotune(20, cache)  # served from the cache
+    info = sim.info()
+    assert info.exec_mode == exec_mode
+    assert info.item_width == 1 << shape[0]
+    assert info.deliver_blocks % shape[1] == 0 and info.pull_summary == shape[2]
+    if exec_mode == sg.EXEC_PERSISTENT:
+        assert info.step_kernel == (3 if prop == sg.PROP_CSR else 2)
+        assert info.spike_ahead == (shape[3] if prop == sg.PROP_CSR else 0)
+    steps = 300
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
+    exp = _oracle(net, 3, steps)
+    _assert_same(sim, (counts, ids, offs), sim.state(), exp)
+    sim.close()
