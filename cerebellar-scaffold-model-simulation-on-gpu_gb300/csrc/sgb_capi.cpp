@@ -323,6 +323,7 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
   info->deliver_blocks = s.deliver_blocks;
   info->pull_summary = (int32_t)s.args.pull_sum;
   info->spike_ahead = info->step_kernel == SGB_KERNEL_FUSED && s.cfg.substeps == 1 && s.args.ahead;
+  info->lane_cells = (int32_t)s.args.lane_cells;
   info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;
   info->weight_type = s.cfg.weight_type;

@@ -182,6 +182,7 @@ struct StepArgs {
   uint32_t max_delay;             // longest synaptic delay, steps (ring_slots = max_delay + 2)
   uint32_t item_log2;             // fused persistent kernel: push items of 2^item_log2 synapses
   uint32_t ahead;                 // fused persistent kernel: spike-ahead timeline (one substep)
+  uint32_t lane_cells;            // general persistent kernel, one-barrier form: cells per lane (1, 2)
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
   uint32_t stdp_early;            // every plastic rule reads only earlier steps' spikes (Teacher)
@@ -232,5 +233,6 @@ size_t pull_async_smem_bytes(const StepArgs& a);  // k_pull_async: summary + ent
 size_t seg_smem_bytes(const StepArgs& a);  // shared memory of the segment descriptors
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
 int persistent_kernel_kind(const StepArgs& a, int blocks);
+bool general_one_barrier(const StepArgs& a);  // the general kernel's one-barrier form applies
 
 }  // namespace sgb

@@ -646,15 +646,17 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.bar_extra = (uint32_t)cfg.barrier_test_extra;
   s.deliver_blocks = 2 * s.sm_count;
   a.item_log2 = 6;  // push items of 64 synapses (the autotuner may pick 32 or 128)
-  a.ahead = 1;      // spike-ahead timeline of the fused kernel (one-substep steps)
-  // Dense pulls settle entries on the staged summary where it fits, and the
-  // per-step pull kernel also stages its entry stream where that fits too.
+  a.ahead = 0;      // fused kernel: spikes in their own step (the autotuner may pick spike-ahead)
+  a.lane_cells = 1;  // general kernel: one cell per lane (the autotuner may pick two)
+  // Dense pulls settle entries on the staged summary where it fits; the
+  // per-step pull kernel may also stage its entry stream (the autotuner's
+  // choice, where that fits too).
+  s.pull_sum_fits = a.pull_sum;
   {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device);
-    if (a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin) a.pull_sum = 2u;
+    if (a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin) s.pull_sum_fits = 2u;
   }
-  s.pull_sum_fits = a.pull_sum;
   // The cell state is read and rewritten every step; where the device lets
   // this context set L2 aside for persisting accesses, the state window
   // stays in L2 across steps while ring slots, tables and history stream
@@ -1155,11 +1157,12 @@ struct TuneShape {
   int32_t deliver_mult;  // per-step driver: delivery blocks per SM
   int32_t pull_sum;      // dense pulls: 0 no summary, 1 staged summary, 2 also staged entries
   int32_t ahead;         // fused kernel: 1 spike-ahead timeline, 0 spikes in their own step
+  int32_t lane_cells;    // general kernel's one-barrier form: cells per lane (1 or 2)
 };
 
 static TuneShape current_shape(const Sim& s) {
   return {(int32_t)s.args.item_log2, std::max(1, s.deliver_blocks / std::max(1, s.sm_count)),
-          (int32_t)s.args.pull_sum, (int32_t)s.args.ahead};
+          (int32_t)s.args.pull_sum, (int32_t)s.args.ahead, (int32_t)s.args.lane_cells};
 }
 
 // Applies a shape (kept within what the handle supports); captured graphs
@@ -1169,6 +1172,7 @@ static void apply_shape(Sim& s, const TuneShape& t) {
   s.deliver_blocks = std::min(8, std::max(1, t.deliver_mult)) * s.sm_count;
   s.args.pull_sum = (uint32_t)std::min<int32_t>(std::max(0, t.pull_sum), (int32_t)s.pull_sum_fits);
   s.args.ahead = t.ahead ? 1u : 0u;
+  s.args.lane_cells = t.lane_cells == 2 ? 2u : 1u;
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
 }
@@ -1198,9 +1202,9 @@ static bool tune_cache_read(const char* path, const std::string& sig, int32_t* e
     }
     const char* sh = strstr(line, "\"shape\": [");
     if (sh && shape) {
-      int32_t v[4] = {6, 2, 1, 1};
-      if (sscanf(sh + 10, "%d , %d , %d , %d", &v[0], &v[1], &v[2], &v[3]) >= 3)
-        *shape = {v[0], v[1], v[2], v[3]};
+      int32_t v[5] = {6, 2, 1, 1, 1};
+      if (sscanf(sh + 10, "%d , %d , %d , %d , %d", &v[0], &v[1], &v[2], &v[3], &v[4]) >= 3)
+        *shape = {v[0], v[1], v[2], v[3], v[4]};
     }
     found = true;
   }
@@ -1216,8 +1220,8 @@ static void tune_cache_write(const char* path, const std::string& sig, int32_t e
   if (!f) return;
   fprintf(f, "{\"signature\": \"%s\", \"exec_mode\": %d, \"modes\": [", sig.c_str(), exec_mode);
   for (size_t i = 0; i < modes.size(); ++i) fprintf(f, "%s%d", i ? ", " : "", modes[i]);
-  fprintf(f, "], \"shape\": [%d, %d, %d, %d], \"us_per_step\": %.4f}\n", shape.item_log2,
-          shape.deliver_mult, shape.pull_sum, shape.ahead, us_per_step);
+  fprintf(f, "], \"shape\": [%d, %d, %d, %d, %d], \"us_per_step\": %.4f}\n", shape.item_log2,
+          shape.deliver_mult, shape.pull_sum, shape.ahead, shape.lane_cells, us_per_step);
   fclose(f);
 }
 
@@ -1328,16 +1332,21 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
     const bool persistent = s.cfg.exec_mode == SGB_EXEC_PERSISTENT;
     if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_FUSED &&
         s.cfg.substeps == 1) {
-      for (int32_t w : {5, 7}) cands.push_back({w, cur.deliver_mult, cur.pull_sum, 1});
-      cands.push_back({6, cur.deliver_mult, cur.pull_sum, 0});  // the other timeline
+      for (int32_t w : {5, 7}) cands.push_back({w, cur.deliver_mult, cur.pull_sum, 1, cur.lane_cells});
+      cands.push_back({6, cur.deliver_mult, cur.pull_sum, 0, cur.lane_cells});  // the other timeline
     }
+    if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_GENERAL &&
+        general_one_barrier(s.args) && s.args.n_plast == 0)
+      cands.push_back({cur.item_log2, cur.deliver_mult, cur.pull_sum, cur.ahead,
+                       3 - cur.lane_cells});  // one or two cells per lane
     if (!persistent)
-      for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead});
-    // Pull variants below the default: without staged entries, without summary.
-    for (int32_t ps = (int32_t)s.pull_sum_fits - 1; s.args.n_pull_units && ps >= 0; --ps)
-      cands.push_back({-1 - ps, -1, -1, -1});
+      for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead, cur.lane_cells});
+    // The other dense-pull variants: no summary, summary, summary and staged entries.
+    for (int32_t ps = 0; s.args.n_pull_units && ps <= (int32_t)s.pull_sum_fits; ++ps)
+      if (ps != cur.pull_sum) cands.push_back({-1 - ps, -1, -1, -1, -1});
     for (TuneShape c : cands) {
-      if (c.item_log2 < 0) c = {cur.item_log2, cur.deliver_mult, -1 - c.item_log2, cur.ahead};
+      if (c.item_log2 < 0)
+        c = {cur.item_log2, cur.deliver_mult, -1 - c.item_log2, cur.ahead, cur.lane_cells};
       apply_shape(s, c);
       double us = 0;
       if ((rc = measure(&us))) return fail(rc);

@@ -415,6 +415,185 @@ __device__ __forceinline__ uint32_t update_words(const StepArgs& a, uint32_t gw,
   return walked;
 }
 
+// ---- two cells per lane (general persistent kernel, one-barrier form) ----------
+// A pair is two consecutive words, cells 64p .. 64p + 63; lane L takes cells
+// 64p + 2L and 64p + 2L + 1, both in word 2p + (L >> 4), so a lane's two cells
+// share a segment (segments start on 32-cell boundaries).  A lane moves its
+// cells' ring entries, potentials and conductances as one int4, float2 and
+// float4 each, and the per-word work -- segment header, LIF constants, bitmap
+// words, counts, push items -- is shared by twice the cells.  Each cell's
+// arithmetic is exactly the one-cell form's.
+struct PairIn {
+  int4 acc;      // {exc, inh} of the lane's two cells
+  float4 g;      // {g0, g1} of the two cells
+  float2 u;      // stored potential fields of the two cells
+  uint32_t seg;  // segment of the lane's word
+};
+
+__device__ __forceinline__ PairIn load_pair(const StepArgs& a, uint32_t p, const StepIdx& ix) {
+  const uint32_t c = (p << 6) + 2u * (threadIdx.x & 31u);
+  PairIn in;
+  in.seg = __ldg(a.seg_of_word + (c >> 5));
+  // ix.roff and c are even: 16-byte aligned pairs of int2 / float2.
+  in.acc = __ldcg(reinterpret_cast<const int4*>(reinterpret_cast<const int2*>(a.ring) + (ix.roff + c)));
+  in.u = __ldcg(reinterpret_cast<const float2*>(a.su + c));
+  in.g = __ldcg(reinterpret_cast<const float4*>(a.sg + c));
+  return in;
+}
+
+// Bitmap words of words w, w + 1 (w even, so both share a summary word).
+__device__ __forceinline__ void put_hist2(const StepArgs& a, const StepIdx& ix, uint32_t w,
+                                          uint32_t b0, uint32_t b1) {
+  __stcg(reinterpret_cast<uint2*>(a.hist + (ix.hoff + w)), make_uint2(b0, b1));
+  __stcg(reinterpret_cast<uint2*>(a.hist + (ix.hoff2 + w)), make_uint2(b0, b1));
+  const uint32_t sbits = (b0 ? 1u << (w & 31u) : 0u) | (b1 ? 2u << (w & 31u) : 0u);
+  if (sbits) atomicOr(a.hsum + (size_t)ix.srow * a.n_swords + (w >> 5), sbits);
+}
+
+// Spike bookkeeping of a pair: bitmap words, per-segment counts (one per
+// word), events, raster entries, and the spiking cells' push rows cut into
+// kPushChunk items in the block's list (items past its capacity are pushed
+// here).  Returns the synapses pushed here.
+template <bool BF16>
+__device__ __forceinline__ uint32_t publish_pair(const StepArgs& a, uint32_t p, uint32_t c,
+                                                 uint32_t seg, bool f0, bool f1, const StepIdx& ix,
+                                                 BlockItems bi) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t packed = (f0 ? 1u : 0u) | (f1 ? 2u : 0u);
+  // Cell j of word 2p is lane j >> 1's cell j & 1; of word 2p + 1, lane 16 + (j >> 1)'s.
+  const uint32_t x0 = __shfl_sync(kFull, packed, lane >> 1);
+  const uint32_t x1 = __shfl_sync(kFull, packed, 16u + (lane >> 1));
+  const uint32_t W0 = __ballot_sync(kFull, (x0 >> (lane & 1u)) & 1u);
+  const uint32_t W1 = __ballot_sync(kFull, (x1 >> (lane & 1u)) & 1u);
+  if (lane == 0) put_hist2(a, ix, 2u * p, W0, W1);
+  if ((W0 | W1) == 0u) return 0;
+  Ctl* ctl = a.ctl;
+  const uint32_t mine = lane < 16u ? W0 : W1;
+  if ((lane & 15u) == 0u && mine)
+    atomicAdd(&a.counts[(size_t)ix.rel * a.n_segs + seg], (uint32_t)__popc(mine));
+  uint32_t ev = 0, ra = 0, rb = 0, rc = 0;
+  if (packed) {
+    if (f0) ev += __ldg(a.outdeg + c);
+    if (f1) ev += __ldg(a.outdeg + c + 1u);
+    if (a.any_push) {
+      ra = __ldg(a.push_row + c);
+      rb = __ldg(a.push_row + c + 1u);
+      rc = __ldg(a.push_row + c + 2u);
+    }
+  }
+  ev = __reduce_add_sync(kFull, ev);
+  const uint32_t na = f0 ? (rb - ra + kPushChunk - 1) / kPushChunk : 0u;
+  const uint32_t nb = f1 ? (rc - rb + kPushChunk - 1) / kPushChunk : 0u;
+  const uint32_t nit = na + nb;
+  uint32_t incl = nit;
+  uint32_t rk = (f0 ? 1u : 0u) + (f1 ? 1u : 0u), rincl = rk;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(kFull, incl, o);
+    const uint32_t r = __shfl_up_sync(kFull, rincl, o);
+    if (lane >= (uint32_t)o) {
+      incl += v;
+      rincl += r;
+    }
+  }
+  const uint32_t tot_items = __shfl_sync(kFull, incl, 31);
+  uint32_t off = 0, roff = 0;
+  if (lane == 0) {
+    if (tot_items) off = atomicAdd(bi.count, tot_items);
+    if (ev) atomicAdd(&ctl->events, (unsigned long long)ev);
+    if (a.raster_cap) roff = atomicAdd(&ctl->raster_count, (uint32_t)(__popc(W0) + __popc(W1)));
+  }
+  off = __shfl_sync(kFull, off, 0) + incl - nit;
+  for (uint32_t k = 0; k < nit && off + k < kGenItems; ++k) {
+    const uint32_t q0 = k < na ? ra + k * kPushChunk : rb + (k - na) * kPushChunk;
+    const uint32_t q1 = k < na ? rb : rc;
+    bi.items[off + k] = make_uint2(q0, min(kPushChunk, q1 - q0) << 23);
+  }
+  uint32_t walked = 0;
+  uint32_t spill = __ballot_sync(kFull, off + nit > kGenItems);
+  while (spill) {
+    const int src = __ffs(spill) - 1;
+    spill &= spill - 1;
+    const uint32_t o = __shfl_sync(kFull, off, src), cnt = __shfl_sync(kFull, nit, src);
+    const uint32_t sa = __shfl_sync(kFull, na, src);
+    const uint32_t pa = __shfl_sync(kFull, ra, src), pb = __shfl_sync(kFull, rb, src),
+                   pc = __shfl_sync(kFull, rc, src);
+    for (uint32_t k = o < kGenItems ? kGenItems - o : 0u; k < cnt; ++k) {
+      const uint32_t q0 = k < sa ? pa + k * kPushChunk : pb + (k - sa) * kPushChunk;
+      const uint32_t q1 = k < sa ? pb : pc;
+      walked += push_item<BF16>(a, make_uint2(q0, min(kPushChunk, q1 - q0) << 23), ix.slot);
+    }
+  }
+  if (a.raster_cap) {
+    roff = __shfl_sync(kFull, roff, 0) + rincl - rk;
+    uint32_t q = roff;
+    if (f0) {
+      if (q < a.raster_cap) a.raster[q] = c; else atomicOr(&ctl->error, kErrRasterOverflow);
+      ++q;
+    }
+    if (f1) {
+      if (q < a.raster_cap) a.raster[q] = c + 1u; else atomicOr(&ctl->error, kErrRasterOverflow);
+    }
+  }
+  return walked;
+}
+
+template <bool SEGSMEM, bool BF16>
+__device__ __forceinline__ uint32_t finish_pair(const StepArgs& a, uint32_t p, const PairIn& in,
+                                                const StepIdx& ix, BlockItems bi) {
+  const uint32_t c = (p << 6) + 2u * (threadIdx.x & 31u);
+  bool f0 = false, f1 = false;
+  if (in.seg != 0xFFFFu) {  // padding words past the last segment (half-warp uniform)
+    const SegDev& sd = SEGSMEM ? reinterpret_cast<const SegDev*>(g_dyn)[in.seg] : a.segs[in.seg];
+    const uint4 hd = *reinterpret_cast<const uint4*>(&sd);  // base, count, key_base, kind
+    const uint32_t l0 = c - hd.x;
+    const bool v0 = l0 < hd.y, v1 = l0 + 1u < hd.y;
+    if (hd.w == kSegInput) {
+      const SrcDev* srcs =
+          SEGSMEM ? reinterpret_cast<const SrcDev*>(g_dyn + seg_table_bytes(a.n_segs)) : a.srcs;
+      const uint2 m = v0 ? __ldg(reinterpret_cast<const uint2*>(a.src_mask + c)) : make_uint2(0u, 0u);
+      if (m.x) f0 = input_fire(a, srcs, sd, l0, m.x, ix.t);
+      if (v1 && m.y) f1 = input_fire(a, srcs, sd, l0 + 1u, m.y, ix.t);
+    } else {
+      // Both lanes' cells run the LIF step (a padding cell integrates its own,
+      // never read, padding state and is masked out of the spikes).
+      if (in.acc.x | in.acc.y | in.acc.z | in.acc.w)
+        __stcg(reinterpret_cast<int4*>(reinterpret_cast<int2*>(a.ring) + (ix.roff + c)),
+               make_int4(0, 0, 0, 0));
+      const LifK k = lif_k(sd);
+      float4 s0 = state_in(in.u.x, make_float2(in.g.x, in.g.y), k.Vr);
+      float4 s1 = state_in(in.u.y, make_float2(in.g.z, in.g.w), k.Vr);
+      f0 = lif_step(k, a.substeps, s0, make_int2(in.acc.x, in.acc.y)) && v0;
+      f1 = lif_step(k, a.substeps, s1, make_int2(in.acc.z, in.acc.w)) && v1;
+      __stcg(reinterpret_cast<float2*>(a.su + c),
+             make_float2(pack_u(s0.x, __float_as_int(s0.w)), pack_u(s1.x, __float_as_int(s1.w))));
+      __stcg(reinterpret_cast<float4*>(a.sg + c), make_float4(s0.y, s0.z, s1.y, s1.z));
+    }
+  }
+  return publish_pair<BF16>(a, p, c, in.seg, f0, f1, ix, bi);
+}
+
+// Pairs gp, gp + np, ... with the next pair's loads in flight while the
+// current one is computed.  Returns the synapses pushed on the way.
+template <bool SEGSMEM, bool BF16>
+__device__ __forceinline__ uint32_t update_pairs(const StepArgs& a, uint32_t gp, uint32_t np,
+                                                 const StepIdx& ix, BlockItems bi) {
+  const uint32_t n_pairs = a.n_words >> 1;
+  uint32_t p = gp, walked = 0;
+  if (p >= n_pairs) return 0;
+  PairIn cur = load_pair(a, p, ix);
+  while (true) {
+    const uint32_t pn = p + np;
+    PairIn nxt;
+    if (pn < n_pairs) nxt = load_pair(a, pn, ix);
+    walked += finish_pair<SEGSMEM, BF16>(a, p, cur, ix, bi);
+    if (pn >= n_pairs) break;
+    p = pn;
+    cur = nxt;
+  }
+  return walked;
+}
+
 // ---- phase 2: deliveries ------------------------------------------------------
 // One warp delivers one push item (at most kPushChunk synapses of a spiking
 // cell's row): all loads of the item are issued before its atomics so the
@@ -474,6 +653,20 @@ __device__ __forceinline__ const uint32_t* hist_base(const StepArgs& a, uint32_t
   return a.hist + (size_t)(a.hist_rows - 1u - hrow) * a.n_words;  // row of step t
 }
 
+// The dense entry stream is read once per step and is larger than L2: its
+// loads carry an evict-first L2 policy, so the lines they bring in go before
+// the spike history, summary and ring lines that the step's pulls reuse.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint32_t ld_entry(const uint32_t* p, uint64_t pol) {
+  uint32_t v;
+  asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+
 template <bool BF16>
 __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, uint32_t o,
                                          uint32_t slot1) {
@@ -506,8 +699,9 @@ __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit 
   {
     const uint32_t ob = o0 + lane;
     uint32_t e[B];
+    const uint64_t pol = l2_evict_first();
 #pragma unroll
-    for (uint32_t u = 0; u < B; ++u) e[u] = __ldg(P.ell_syn + ob + 32u * u);  // padded to units
+    for (uint32_t u = 0; u < B; ++u) e[u] = ld_entry(P.ell_syn + ob + 32u * u, pol);  // padded to units
     uint32_t hit = 0;
     if (s_sum) {
       // The block's staged summary settles most entries; the history word is
@@ -681,11 +875,12 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
   const StepIdx ix = step_of(a);
   const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
   uint32_t e[E];
+  const uint64_t pol = l2_evict_first();
   if (gw < n) {
     const PullUnit un = a.pull_units[gw];
     const uint32_t* src = a.projs[un.proj].ell_syn + un.o0 + lane;
 #pragma unroll
-    for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
+    for (uint32_t k = 0; k < E; ++k) e[k] = ld_entry(src + k * 32u, pol);
   }
   if (SUM) {
     stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
@@ -700,7 +895,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
     const uint32_t* src = P.ell_syn + un.o0 + lane;  // tables are padded to whole units
     if (u != gw) {
 #pragma unroll
-      for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
+      for (uint32_t k = 0; k < E; ++k) e[k] = ld_entry(src + k * 32u, pol);
     }
     uint32_t need = 0;
 #pragma unroll
@@ -1139,7 +1334,8 @@ __device__ void raster_offsets_from_counts(const StepArgs& a, uint32_t n_steps, 
 // spiking cells' push items in shared memory during the update, delivers them
 // right after it, and one grid barrier ends the step.  Otherwise the items go
 // to a global list delivered by all warps between two grid barriers.
-template <bool BF16, bool ONE>
+// PAIRS (one-barrier form, no plasticity): two cells per lane (update_pairs).
+template <bool BF16, bool ONE, bool PAIRS = false>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
   // Dynamic shared memory: the segment descriptors every word reads (when
   // a.seg_smem), then the staged spike summary (dense pulls, when it fits).
@@ -1184,6 +1380,9 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     if (a.n_plast)
       walked += a.seg_smem ? update_words<true, true, BF16, ONE>(a, uw, nw, ix, bi)
                            : update_words<true, false, BF16, ONE>(a, uw, nw, ix, bi);
+    else if (PAIRS)
+      walked += a.seg_smem ? update_pairs<true, BF16>(a, uw, nw, ix, bi)
+                           : update_pairs<false, BF16>(a, uw, nw, ix, bi);
     else
       walked += a.seg_smem ? update_words<false, true, BF16, ONE>(a, uw, nw, ix, bi)
                            : update_words<false, false, BF16, ONE>(a, uw, nw, ix, bi);
@@ -1853,6 +2052,8 @@ cudaError_t pull_setup() {
   if ((e = cudaFuncSetAttribute(k_persistent<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent_resident<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)))
     return e;
   return cudaFuncSetAttribute(k_persistent_resident<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -1900,11 +2101,17 @@ int persistent_blocks_per_sm(bool bf16) {
   int o = 0;
   if (bf16) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<true, true>, kPersistBlock, 0);
+    int q = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_persistent<true, true, true>, kPersistBlock, 0);
+    o = o < q ? o : q;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
     f = fused_blocks_per_sm();
   } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<false, true>, kPersistBlock, 0);
+    int q = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_persistent<false, true, true>, kPersistBlock, 0);
+    o = o < q ? o : q;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
     f = fused_blocks_per_sm();
@@ -1937,7 +2144,11 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
                                         : (const void*)k_persistent_resident<false>)
                    : general_one_barrier(a)
-                       ? (a.bf16 ? (const void*)k_persistent<true, true> : (const void*)k_persistent<false, true>)
+                       ? (a.n_plast == 0 && a.lane_cells == 2u
+                              ? (a.bf16 ? (const void*)k_persistent<true, true, true>
+                                        : (const void*)k_persistent<false, true, true>)
+                              : (a.bf16 ? (const void*)k_persistent<true, true>
+                                        : (const void*)k_persistent<false, true>))
                        : (a.bf16 ? (const void*)k_persistent<true, false>
                                  : (const void*)k_persistent<false, false>);
   const size_t smem = fused ? a.row_smem

@@ -88,7 +88,8 @@ class SimInfo(C.Structure):
                 ("pull_entries", C.c_int64), ("l2_persist_bytes", C.c_int64),
                 ("shard_cells", C.c_int64), ("item_width", C.c_int32),
                 ("deliver_blocks", C.c_int32), ("pull_summary", C.c_int32),
-                ("spike_ahead", C.c_int32)]
+                ("spike_ahead", C.c_int32), ("lane_cells", C.c_int32),
+                ("reserved_", C.c_int32)]
 
 
 P = C.POINTER

@@ -177,6 +177,8 @@ typedef struct sgb_sim_info {
                           /* settle on a staged spike summary; 2 as 1, the per-step pull  */
                           /* also staging its entry stream in shared memory               */
   int32_t spike_ahead;    /* SGB_KERNEL_FUSED: 1 the spike-ahead timeline (one substep)   */
+  int32_t lane_cells;     /* SGB_KERNEL_GENERAL, one-barrier form: cells per lane (1, 2)  */
+  int32_t reserved_;
 } sgb_sim_info;
 
 /* Step kernels (sgb_sim_info.step_kernel). */

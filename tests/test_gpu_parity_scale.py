@@ -56,6 +56,25 @@ def _assert_instance(k, nets, seeds, counts, ids, offs, state, steps, bf16):
     return int(ec.sum())
 
 
+def _with_shape(nets, seeds, shape, modes, exec_mode, tmp_path, **kw):
+    """A handle whose driver, propagation modes and launch shape are the
+    given ones: a first handle tunes briefly to write the cache line for
+    this network, the line is edited, and a second handle serves from it."""
+    import json
+
+    cache = str(tmp_path / "tune.jsonl")
+    first = sg.Simulation(nets, seeds, **kw)
+    first.autotune(5, cache)
+    first.close()
+    line = json.loads(open(cache).read().splitlines()[0])
+    line.update(exec_mode=exec_mode, modes=modes, shape=shape)
+    with open(cache, "w") as f:
+        f.write(json.dumps(line) + "\n")
+    sim = sg.Simulation(nets, seeds, **kw)
+    sim.autotune(5, cache)
+    return sim
+
+
 def _assert_same(counts, ids, offs, state, exp):
     ecounts, eids, eoffs, eu, eg, eref, _ = exp
     u, g, ref = state
@@ -102,15 +121,19 @@ def test_config3_bf16_push_fused():
     sim.close()
 
 
-def test_config4_batch_of_64_scaled_instances():
+@pytest.mark.parametrize("lane_cells", [1, 2])
+def test_config4_batch_of_64_scaled_instances(tmp_path, lane_cells):
+    """lane_cells 2: the general kernel's two-cells-per-lane update."""
     seeds = [1 + k for k in range(64)]
     scales = sg.batched_scales(seeds)
     nets = [sg.scaffold(2, sc, sd) for sc, sd in zip(scales, seeds)]
     steps = 200
-    sim = sg.Simulation(nets, seeds, weight_type=sg.WEIGHT_BF16, exec_mode=sg.EXEC_PERSISTENT,
-                        raster=True, chunk_steps=100)
+    sim = _with_shape(nets, seeds, [6, 2, 1, 0, lane_cells],
+                      [sg.PROP_CSR] * sum(len(n.projections) for n in nets), sg.EXEC_PERSISTENT,
+                      tmp_path, weight_type=sg.WEIGHT_BF16, raster=True, chunk_steps=100)
     info = sim.info()
     assert info.step_kernel == 1  # SGB_KERNEL_GENERAL: more words than resident warps
+    assert info.lane_cells == lane_cells
     assert info.n_synapses > 150_000_000
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True, raster_cap=1 << 24)
     state = sim.state()
@@ -171,4 +194,29 @@ def test_many_segments_against_the_oracle():
     for k in (0, 1, 77, 124, 125, 200, 248, 249):
         spikes += _assert_instance(k, nets, seeds, counts, ids, offs, state, steps, False)
     assert spikes > 0
+    sim.close()
+
+
+@pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
+def test_two_cells_per_lane_general_kernel(tmp_path, weight):
+    """Config 1 at 20x (185,120 cells; its DCN segment is five words long, so
+    pairs of words straddle segment ends and a warp's two halves run different
+    segments, even an input and a LIF segment) plus a second, smaller
+    instance, through the general kernel with two cells per lane."""
+    nets = [sg.scaffold(1, 20.0, 21), sg.scaffold(1, 3.3, 22)]
+    seeds = [21, 22]
+    steps = 240
+    sim = _with_shape(nets, seeds, [6, 2, 1, 0, 2],
+                      [sg.PROP_CSR] * sum(len(n.projections) for n in nets), sg.EXEC_PERSISTENT,
+                      tmp_path, weight_type=weight, raster=True, chunk_steps=120)
+    info = sim.info()
+    assert info.step_kernel == 1 and info.lane_cells == 2
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True, raster_cap=1 << 22)
+    state = sim.state()
+    spikes = 0
+    for k in range(2):
+        spikes += _assert_instance(k, nets, seeds, counts, ids, offs, state, steps,
+                                   weight == sg.WEIGHT_BF16)
+    assert spikes > 0
+    assert sim.info().delivered > 0
     sim.close()
