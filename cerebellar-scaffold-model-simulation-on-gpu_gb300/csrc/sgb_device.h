@@ -191,7 +191,8 @@ struct StepArgs {
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
   uint32_t pull_sum;              // dense pulls: 0 every entry loads its history word; 1 entries
                                   // settle on a staged spike summary; 2 as 1, the per-step
-                                  // kernel also staging its entry stream (k_pull_async)
+                                  // kernel also staging its entry stream (k_pull_async); 3 as 1,
+                                  // the per-step kernel loading entries 16 bytes at a time
   uint32_t any_push;
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer

@@ -647,15 +647,15 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   s.deliver_blocks = 2 * s.sm_count;
   a.item_log2 = 6;  // push items of 64 synapses (the autotuner may pick 32 or 128)
   a.ahead = 0;      // fused kernel: spikes in their own step (the autotuner may pick spike-ahead)
-  a.lane_cells = 1;  // general kernel: one cell per lane (the autotuner may pick two)
+  a.lane_cells = 2;  // general kernel, one-barrier form: two cells per lane (or one: autotuner)
   // Dense pulls settle entries on the staged summary where it fits; the
   // per-step pull kernel may also stage its entry stream (the autotuner's
   // choice, where that fits too).
-  s.pull_sum_fits = a.pull_sum;
+  s.pull_sum_fits = a.pull_sum != 0;
   {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device);
-    if (a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin) s.pull_sum_fits = 2u;
+    s.pull_async_fits = a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin;
   }
   // The cell state is read and rewritten every step; where the device lets
   // this context set L2 aside for persisting accesses, the state window
@@ -1170,7 +1170,9 @@ static TuneShape current_shape(const Sim& s) {
 static void apply_shape(Sim& s, const TuneShape& t) {
   s.args.item_log2 = (uint32_t)std::min(7, std::max(5, t.item_log2));
   s.deliver_blocks = std::min(8, std::max(1, t.deliver_mult)) * s.sm_count;
-  s.args.pull_sum = (uint32_t)std::min<int32_t>(std::max(0, t.pull_sum), (int32_t)s.pull_sum_fits);
+  const bool ok = t.pull_sum == 0 || (s.pull_sum_fits && t.pull_sum >= 1 && t.pull_sum <= 3 &&
+                                      (t.pull_sum != 2 || s.pull_async_fits));
+  s.args.pull_sum = ok ? (uint32_t)t.pull_sum : (s.pull_sum_fits ? 1u : 0u);
   s.args.ahead = t.ahead ? 1u : 0u;
   s.args.lane_cells = t.lane_cells == 2 ? 2u : 1u;
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
@@ -1341,9 +1343,12 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
                        3 - cur.lane_cells});  // one or two cells per lane
     if (!persistent)
       for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead, cur.lane_cells});
-    // The other dense-pull variants: no summary, summary, summary and staged entries.
-    for (int32_t ps = 0; s.args.n_pull_units && ps <= (int32_t)s.pull_sum_fits; ++ps)
-      if (ps != cur.pull_sum) cands.push_back({-1 - ps, -1, -1, -1, -1});
+    // The other dense-pull variants: no summary; summary; summary with staged
+    // entries (per-step kernel); summary with 16-byte entry loads (per-step).
+    for (int32_t ps = 0; s.args.n_pull_units && ps <= 3; ++ps) {
+      const bool ok = ps == 0 || (s.pull_sum_fits && (ps != 2 || s.pull_async_fits));
+      if (ok && ps != cur.pull_sum && (ps < 2 || !persistent)) cands.push_back({-1 - ps, -1, -1, -1, -1});
+    }
     for (TuneShape c : cands) {
       if (c.item_log2 < 0)
         c = {cur.item_log2, cur.deliver_mult, -1 - c.item_log2, cur.ahead, cur.lane_cells};

@@ -653,20 +653,6 @@ __device__ __forceinline__ const uint32_t* hist_base(const StepArgs& a, uint32_t
   return a.hist + (size_t)(a.hist_rows - 1u - hrow) * a.n_words;  // row of step t
 }
 
-// The dense entry stream is read once per step and is larger than L2: its
-// loads carry an evict-first L2 policy, so the lines they bring in go before
-// the spike history, summary and ring lines that the step's pulls reuse.
-__device__ __forceinline__ uint64_t l2_evict_first() {
-  uint64_t pol;
-  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ uint32_t ld_entry(const uint32_t* p, uint64_t pol) {
-  uint32_t v;
-  asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
-  return v;
-}
-
 template <bool BF16>
 __device__ __forceinline__ void pull_hit(const StepArgs& a, const ProjDev& P, uint32_t o,
                                          uint32_t slot1) {
@@ -699,9 +685,8 @@ __device__ __forceinline__ uint32_t pull_unit(const StepArgs& a, const PullUnit 
   {
     const uint32_t ob = o0 + lane;
     uint32_t e[B];
-    const uint64_t pol = l2_evict_first();
 #pragma unroll
-    for (uint32_t u = 0; u < B; ++u) e[u] = ld_entry(P.ell_syn + ob + 32u * u, pol);  // padded to units
+    for (uint32_t u = 0; u < B; ++u) e[u] = __ldg(P.ell_syn + ob + 32u * u);  // padded to units
     uint32_t hit = 0;
     if (s_sum) {
       // The block's staged summary settles most entries; the history word is
@@ -875,12 +860,11 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
   const StepIdx ix = step_of(a);
   const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
   uint32_t e[E];
-  const uint64_t pol = l2_evict_first();
   if (gw < n) {
     const PullUnit un = a.pull_units[gw];
     const uint32_t* src = a.projs[un.proj].ell_syn + un.o0 + lane;
 #pragma unroll
-    for (uint32_t k = 0; k < E; ++k) e[k] = ld_entry(src + k * 32u, pol);
+    for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
   }
   if (SUM) {
     stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
@@ -895,7 +879,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
     const uint32_t* src = P.ell_syn + un.o0 + lane;  // tables are padded to whole units
     if (u != gw) {
 #pragma unroll
-      for (uint32_t k = 0; k < E; ++k) e[k] = ld_entry(src + k * 32u, pol);
+      for (uint32_t k = 0; k < E; ++k) e[k] = __ldg(src + k * 32u);
     }
     uint32_t need = 0;
 #pragma unroll
@@ -924,6 +908,77 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
         if (ks[j] < E && ((hw[j] >> (ev[j] & 31u)) & 1u)) {
           ++hits;
           pull_hit<BF16>(a, P, un.o0 + ks[j] * 32u + lane, slot1);
+        }
+      }
+    }
+  }
+  hits = __reduce_add_sync(kFull, hits);
+  if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
+}
+
+// Dense pull with 16-byte entry loads (per-step driver; one 1,024-thread
+// block per SM): as k_pull with the staged summary, but a lane holds entries
+// 4L .. 4L + 3 of each 128-entry row of its unit and loads them as one uint4,
+// eight loads per unit instead of 32.  Entry m of the lane (0 .. 31) is at
+// unit offset (m >> 2) * 128 + 4L + (m & 3).
+template <bool BF16>
+__global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
+  constexpr uint32_t V = kPullUnit / 128;  // 16-byte loads per lane per unit
+  constexpr uint32_t E = 4 * V;            // entries per lane per unit
+  constexpr uint32_t W = 4;                // entries walked per trip
+  extern __shared__ uint32_t s_sum[];      // [H][n_swords] + 1 (padding's word)
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
+  const uint32_t n = a.n_pull_units;
+  const StepIdx ix = step_of(a);
+  const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+  uint4 q[V];
+  if (gw < n) {
+    const PullUnit un = a.pull_units[gw];
+    const uint4* src = reinterpret_cast<const uint4*>(a.projs[un.proj].ell_syn + un.o0) + lane;
+#pragma unroll
+    for (uint32_t k = 0; k < V; ++k) q[k] = __ldg(src + 32u * k);
+  }
+  stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
+  __syncthreads();
+  const uint32_t* hb = hist_base(a, ix.hrow);
+  uint32_t hits = 0;
+  for (uint32_t u = gw; u < n; u += nw) {
+    const PullUnit un = a.pull_units[u];
+    const ProjDev& P = a.projs[un.proj];
+    const uint32_t* base = P.ell_syn + un.o0 + 4u * lane;  // tables are padded to whole units
+    if (u != gw) {
+#pragma unroll
+      for (uint32_t k = 0; k < V; ++k) q[k] = __ldg(reinterpret_cast<const uint4*>(base) + 32u * k);
+    }
+    uint32_t need = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < V; ++k) {
+      const uint32_t ev4[4] = {q[k].x, q[k].y, q[k].z, q[k].w};
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) {
+        const uint32_t sw = s_sum[ev4[j] >> 10];
+        need |= (__funnelshift_r(sw, sw, ev4[j] >> 5) & 1u) << (4u * k + j);
+      }
+    }
+    while (need) {
+      uint32_t ms[W], ev[W], hw[W];
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) {
+        ms[j] = need ? __ffs(need) - 1u : E;
+        need &= need - 1u;
+      }
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j)
+        ev[j] = ms[j] < E ? __ldg(base + (ms[j] >> 2) * 128u + (ms[j] & 3u)) : 0u;
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) hw[j] = ms[j] < E ? __ldg(hb + (ev[j] >> 5)) : 0u;
+#pragma unroll
+      for (uint32_t j = 0; j < W; ++j) {
+        if (ms[j] < E && ((hw[j] >> (ev[j] & 31u)) & 1u)) {
+          ++hits;
+          pull_hit<BF16>(a, P, un.o0 + (ms[j] >> 2) * 128u + 4u * lane + (ms[j] & 3u), slot1);
         }
       }
     }
@@ -1997,6 +2052,12 @@ size_t pull_async_smem_bytes(const StepArgs& a) {
 
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
   if (!a.n_pull_units) return cudaSuccess;
+  if (a.pull_sum == 3u) {
+    const size_t smem = pull_sum_bytes(a);
+    if (a.bf16) k_pull_vec<true><<<blocks, kPullBlock, smem, s>>>(a);
+    else k_pull_vec<false><<<blocks, kPullBlock, smem, s>>>(a);
+    return cudaGetLastError();
+  }
   if (a.pull_sum == 2u) {
     const size_t smem = pull_async_smem_bytes(a);
     if (a.bf16) k_pull_async<true><<<blocks, kPullBlock, smem, s>>>(a);
@@ -2041,6 +2102,8 @@ cudaError_t pull_setup() {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if ((e = cudaFuncSetAttribute(k_pull_vec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_pull_vec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_async<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_async<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
