@@ -652,6 +652,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   // per-step pull kernel may also stage its entry stream (the autotuner's
   // choice, where that fits too).
   s.pull_sum_fits = a.pull_sum != 0;
+  if (a.pull_sum) a.pull_sum = 3u;  // summary staged; the per-step pull loads entries 16 B at a time
   {
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device);
