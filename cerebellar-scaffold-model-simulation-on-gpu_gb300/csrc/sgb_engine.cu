@@ -657,6 +657,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device);
     s.pull_async_fits = a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin;
+    // (with room for the kernel's 8.5 KB of static shared memory)
+    s.pair_stage_fits = pair_stage_smem_bytes(a) + 16384 <= (size_t)optin;
   }
   // The cell state is read and rewritten every step; where the device lets
   // this context set L2 aside for persisting accesses, the state window
@@ -1175,7 +1177,7 @@ static void apply_shape(Sim& s, const TuneShape& t) {
                                       (t.pull_sum != 2 || s.pull_async_fits));
   s.args.pull_sum = ok ? (uint32_t)t.pull_sum : (s.pull_sum_fits ? 1u : 0u);
   s.args.ahead = t.ahead ? 1u : 0u;
-  s.args.lane_cells = t.lane_cells == 2 ? 2u : 1u;
+  s.args.lane_cells = t.lane_cells == 3 && s.pair_stage_fits ? 3u : (t.lane_cells >= 2 ? 2u : 1u);
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
 }
@@ -1340,8 +1342,9 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
     }
     if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_GENERAL &&
         general_one_barrier(s.args) && s.args.n_plast == 0)
-      cands.push_back({cur.item_log2, cur.deliver_mult, cur.pull_sum, cur.ahead,
-                       3 - cur.lane_cells});  // one or two cells per lane
+      for (int32_t lc = 1; lc <= (s.pair_stage_fits ? 3 : 2); ++lc)  // cells per lane, staging
+        if (lc != cur.lane_cells)
+          cands.push_back({cur.item_log2, cur.deliver_mult, cur.pull_sum, cur.ahead, lc});
     if (!persistent)
       for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead, cur.lane_cells});
     // The other dense-pull variants: no summary; summary; summary with staged

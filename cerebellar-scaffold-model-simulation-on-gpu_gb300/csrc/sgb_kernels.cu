@@ -594,6 +594,61 @@ __device__ __forceinline__ uint32_t update_pairs(const StepArgs& a, uint32_t gp,
   return walked;
 }
 
+// Staged pairs (lane_cells 3): a warp's next kPairStages pairs stream into its
+// shared-memory stages with 16-byte cp.async.cg copies (at L2: ring slots and
+// state are rewritten by other SMs during the launch) -- ring entries (512 B),
+// conductances (512 B) and potentials (256 B) per pair -- so three pairs are
+// in flight per warp without holding registers for them.
+constexpr uint32_t kPairStages = 3;
+constexpr uint32_t kPairStageBytes = 1280;
+constexpr size_t kPairStageBlockBytes = (size_t)(kPersistBlock / 32) * kPairStages * kPairStageBytes;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+template <bool SEGSMEM, bool BF16>
+__device__ __forceinline__ uint32_t update_pairs_staged(const StepArgs& a, uint32_t gp, uint32_t np,
+                                                        const StepIdx& ix, BlockItems bi,
+                                                        unsigned char* stages) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t n_pairs = a.n_words >> 1;
+  const unsigned char* my = stages + (size_t)(threadIdx.x >> 5) * kPairStages * kPairStageBytes;
+  const uint32_t my_s = (uint32_t)__cvta_generic_to_shared(my);
+  // Pair p into stage k: lane L copies its two cells' ring entries and
+  // conductances; lanes 0..15 copy four cells' potentials each.
+  auto issue = [&](uint32_t p, uint32_t k) {
+    if (p < n_pairs) {
+      const uint32_t c = p << 6;
+      const uint32_t d = my_s + k * kPairStageBytes;
+      cp_async16(d + 16u * lane, reinterpret_cast<const int2*>(a.ring) + (ix.roff + c + 2u * lane));
+      cp_async16(d + 512u + 16u * lane, a.sg + c + 2u * lane);
+      if (lane < 16u) cp_async16(d + 1024u + 16u * lane, a.su + c + 4u * lane);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  issue(gp, 0u);
+  issue(gp + np, 1u);
+  issue(gp + 2u * np, 2u);
+  uint32_t walked = 0, k = 0;
+  for (uint32_t p = gp; p < n_pairs; p += np) {
+    asm volatile("cp.async.wait_group 2;" ::: "memory");  // the oldest group is pair p's
+    __syncwarp();
+    const unsigned char* st = my + k * kPairStageBytes;
+    PairIn in;
+    in.acc = *reinterpret_cast<const int4*>(st + 16u * lane);
+    in.g = *reinterpret_cast<const float4*>(st + 512u + 16u * lane);
+    in.u = *reinterpret_cast<const float2*>(st + 1024u + 8u * lane);
+    in.seg = __ldg(a.seg_of_word + (((p << 6) + 2u * lane) >> 5));
+    __syncwarp();  // every lane has read the stage before it is refilled
+    issue(p + 3u * np, k);
+    walked += finish_pair<SEGSMEM, BF16>(a, p, in, ix, bi);
+    k = k + 1u == kPairStages ? 0u : k + 1u;
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  return walked;
+}
+
 // ---- phase 2: deliveries ------------------------------------------------------
 // One warp delivers one push item (at most kPushChunk synapses of a spiking
 // cell's row): all loads of the item are issued before its atomics so the
@@ -1395,12 +1450,16 @@ __device__ void raster_offsets_from_counts(const StepArgs& a, uint32_t n_steps, 
 // spiking cells' push items in shared memory during the update, delivers them
 // right after it, and one grid barrier ends the step.  Otherwise the items go
 // to a global list delivered by all warps between two grid barriers.
-// PAIRS (one-barrier form, no plasticity): two cells per lane (update_pairs).
-template <bool BF16, bool ONE, bool PAIRS = false>
+// LANE (one-barrier form, no plasticity): 1 one cell per lane (update_words),
+// 2 two cells per lane (update_pairs), 3 two cells per lane with the loads
+// staged in shared memory (update_pairs_staged).
+template <bool BF16, bool ONE, int LANE = 1>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
   // Dynamic shared memory: the segment descriptors every word reads (when
   // a.seg_smem), then the staged spike summary (dense pulls, when it fits).
   uint32_t* s_sum = reinterpret_cast<uint32_t*>(g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0));
+  // LANE 3: the warps' pair stages after the segment descriptors.
+  unsigned char* pair_stages = g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0);
   __shared__ uint2 s_items[ONE ? kGenItems : 1];
   __shared__ uint32_t s_icnt[2];  // item count of step parity p; the other one is reset
   __shared__ uint32_t s_wsum[kPersistBlock / 32];
@@ -1441,9 +1500,12 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     if (a.n_plast)
       walked += a.seg_smem ? update_words<true, true, BF16, ONE>(a, uw, nw, ix, bi)
                            : update_words<true, false, BF16, ONE>(a, uw, nw, ix, bi);
-    else if (PAIRS)
+    else if (LANE == 2)
       walked += a.seg_smem ? update_pairs<true, BF16>(a, uw, nw, ix, bi)
                            : update_pairs<false, BF16>(a, uw, nw, ix, bi);
+    else if (LANE == 3)
+      walked += a.seg_smem ? update_pairs_staged<true, BF16>(a, uw, nw, ix, bi, pair_stages)
+                           : update_pairs_staged<false, BF16>(a, uw, nw, ix, bi, pair_stages);
     else
       walked += a.seg_smem ? update_words<false, true, BF16, ONE>(a, uw, nw, ix, bi)
                            : update_words<false, false, BF16, ONE>(a, uw, nw, ix, bi);
@@ -2052,6 +2114,11 @@ size_t seg_smem_bytes(const StepArgs& a) { return seg_smem_bytes_dev(a); }
 static size_t pull_smem_bytes(const StepArgs& a) { return a.pull_sum ? pull_sum_bytes(a) : 0; }
 
 // k_pull_async: the staged summary (rounded to 16 bytes) and the warps' buffers.
+// The general kernel's staged pairs: descriptors and the warps' stages.
+size_t pair_stage_smem_bytes(const StepArgs& a) {
+  return (a.seg_smem ? seg_smem_bytes_dev(a) : 0) + kPairStageBlockBytes;
+}
+
 size_t pull_async_smem_bytes(const StepArgs& a) {
   return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + kPullBufBytes;
 }
@@ -2108,6 +2175,8 @@ cudaError_t pull_setup() {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if ((e = cudaFuncSetAttribute(k_persistent<true, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<false, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_vec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_vec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_async<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
@@ -2121,8 +2190,8 @@ cudaError_t pull_setup() {
   if ((e = cudaFuncSetAttribute(k_persistent<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
-  if ((e = cudaFuncSetAttribute(k_persistent<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
-  if ((e = cudaFuncSetAttribute(k_persistent<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<true, true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
+  if ((e = cudaFuncSetAttribute(k_persistent<false, true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_persistent_resident<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)))
     return e;
   return cudaFuncSetAttribute(k_persistent_resident<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -2171,7 +2240,7 @@ int persistent_blocks_per_sm(bool bf16) {
   if (bf16) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<true, true>, kPersistBlock, 0);
     int q = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_persistent<true, true, true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_persistent<true, true, 2>, kPersistBlock, 0);
     o = o < q ? o : q;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<true, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<true>, kPersistBlock, 0);
@@ -2179,7 +2248,7 @@ int persistent_blocks_per_sm(bool bf16) {
   } else {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_persistent<false, true>, kPersistBlock, 0);
     int q = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_persistent<false, true, true>, kPersistBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_persistent<false, true, 2>, kPersistBlock, 0);
     o = o < q ? o : q;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false, false>, kPersistBlock, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_persistent_resident<false>, kPersistBlock, 0);
@@ -2213,16 +2282,21 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
                                         : (const void*)k_persistent_resident<false>)
                    : general_one_barrier(a)
-                       ? (a.n_plast == 0 && a.lane_cells == 2u
-                              ? (a.bf16 ? (const void*)k_persistent<true, true, true>
-                                        : (const void*)k_persistent<false, true, true>)
+                       ? (a.n_plast == 0 && a.lane_cells == 3u
+                              ? (a.bf16 ? (const void*)k_persistent<true, true, 3>
+                                        : (const void*)k_persistent<false, true, 3>)
+                          : a.n_plast == 0 && a.lane_cells == 2u
+                              ? (a.bf16 ? (const void*)k_persistent<true, true, 2>
+                                        : (const void*)k_persistent<false, true, 2>)
                               : (a.bf16 ? (const void*)k_persistent<true, true>
                                         : (const void*)k_persistent<false, true>))
                        : (a.bf16 ? (const void*)k_persistent<true, false>
                                  : (const void*)k_persistent<false, false>);
+  const bool staged = !resident && general_one_barrier(a) && a.n_plast == 0 && a.lane_cells == 3u;
   const size_t smem = fused ? a.row_smem
                      : (a.seg_smem ? seg_smem_bytes(a) : 0) +
-                           ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0);
+                           ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0) +
+                           (staged ? kPairStageBlockBytes : 0);
   return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, smem, s);
 }
 

@@ -121,9 +121,10 @@ def test_config3_bf16_push_fused():
     sim.close()
 
 
-@pytest.mark.parametrize("lane_cells", [1, 2])
+@pytest.mark.parametrize("lane_cells", [1, 2, 3])
 def test_config4_batch_of_64_scaled_instances(tmp_path, lane_cells):
-    """lane_cells 2: the general kernel's two-cells-per-lane update."""
+    """lane_cells 2: the general kernel's two-cells-per-lane update; 3: the
+    same with each warp's next pairs staged in shared memory."""
     seeds = [1 + k for k in range(64)]
     scales = sg.batched_scales(seeds)
     nets = [sg.scaffold(2, sc, sd) for sc, sd in zip(scales, seeds)]
@@ -197,8 +198,9 @@ def test_many_segments_against_the_oracle():
     sim.close()
 
 
-@pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
-def test_two_cells_per_lane_general_kernel(tmp_path, weight):
+@pytest.mark.parametrize("weight,lane_cells", [(sg.WEIGHT_FP32, 2), (sg.WEIGHT_BF16, 2),
+                                               (sg.WEIGHT_FP32, 3), (sg.WEIGHT_BF16, 3)])
+def test_two_cells_per_lane_general_kernel(tmp_path, weight, lane_cells):
     """Config 1 at 20x (185,120 cells; its DCN segment is five words long, so
     pairs of words straddle segment ends and a warp's two halves run different
     segments, even an input and a LIF segment) plus a second, smaller
@@ -206,11 +208,11 @@ def test_two_cells_per_lane_general_kernel(tmp_path, weight):
     nets = [sg.scaffold(1, 20.0, 21), sg.scaffold(1, 3.3, 22)]
     seeds = [21, 22]
     steps = 240
-    sim = _with_shape(nets, seeds, [6, 2, 1, 0, 2],
+    sim = _with_shape(nets, seeds, [6, 2, 1, 0, lane_cells],
                       [sg.PROP_CSR] * sum(len(n.projections) for n in nets), sg.EXEC_PERSISTENT,
                       tmp_path, weight_type=weight, raster=True, chunk_steps=120)
     info = sim.info()
-    assert info.step_kernel == 1 and info.lane_cells == 2
+    assert info.step_kernel == 1 and info.lane_cells == lane_cells
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True, raster_cap=1 << 22)
     state = sim.state()
     spikes = 0
