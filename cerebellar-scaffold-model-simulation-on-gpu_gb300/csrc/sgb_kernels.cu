@@ -2175,12 +2175,17 @@ cudaError_t pull_setup() {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if ((e = cudaFuncSetAttribute(k_persistent<true, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
-  if ((e = cudaFuncSetAttribute(k_persistent<false, true, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
+  // The opt-in limit covers static and dynamic shared memory together.
+  for (const void* fn : {(const void*)k_persistent<true, true, 3>, (const void*)k_persistent<false, true, 3>,
+                         (const void*)k_pull_async<true>, (const void*)k_pull_async<false>}) {
+    cudaFuncAttributes fa{};
+    if ((e = cudaFuncGetAttributes(&fa, fn))) return e;
+    const int lim = optin - (int)fa.sharedSizeBytes;
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
+  }
   if ((e = cudaFuncSetAttribute(k_pull_vec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_vec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
-  if ((e = cudaFuncSetAttribute(k_pull_async<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
-  if ((e = cudaFuncSetAttribute(k_pull_async<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin))) return e;
+
   if ((e = cudaFuncSetAttribute(k_pull<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
