@@ -975,11 +975,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull(StepArgs a) {
 // block per SM): as k_pull with the staged summary, but a lane holds entries
 // 4L .. 4L + 3 of each 128-entry row of its unit and loads them as one uint4,
 // eight loads per unit instead of 32.  Entry m of the lane (0 .. 31) is at
-// unit offset (m >> 2) * 128 + 4L + (m & 3).  Once a unit's summary test is
-// done its entries are only re-read for the few that passed: the first trip
-// of the walk (up to four per lane, almost always all of them) re-reads them
-// from L1, and then the next unit's loads are issued into the freed registers,
-// so they are in flight while the walk waits for history words and weights.
+// unit offset (m >> 2) * 128 + 4L + (m & 3).
 template <bool BF16>
 __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
   constexpr uint32_t V = kPullUnit / 128;  // 16-byte loads per lane per unit
@@ -993,13 +989,12 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
   const StepIdx ix = step_of(a);
   const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
   uint4 q[V];
-  auto load_unit = [&](uint32_t u) {
-    const PullUnit un = a.pull_units[u];
+  if (gw < n) {
+    const PullUnit un = a.pull_units[gw];
     const uint4* src = reinterpret_cast<const uint4*>(a.projs[un.proj].ell_syn + un.o0) + lane;
 #pragma unroll
     for (uint32_t k = 0; k < V; ++k) q[k] = __ldg(src + 32u * k);
-  };
-  if (gw < n) load_unit(gw);
+  }
   stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
   __syncthreads();
   const uint32_t* hb = hist_base(a, ix.hrow);
@@ -1008,6 +1003,10 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
     const PullUnit un = a.pull_units[u];
     const ProjDev& P = a.projs[un.proj];
     const uint32_t* base = P.ell_syn + un.o0 + 4u * lane;  // tables are padded to whole units
+    if (u != gw) {
+#pragma unroll
+      for (uint32_t k = 0; k < V; ++k) q[k] = __ldg(reinterpret_cast<const uint4*>(base) + 32u * k);
+    }
     uint32_t need = 0;
 #pragma unroll
     for (uint32_t k = 0; k < V; ++k) {
@@ -1018,8 +1017,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
         need |= (__funnelshift_r(sw, sw, ev4[j] >> 5) & 1u) << (4u * k + j);
       }
     }
-    bool first = true;
-    do {
+    while (need) {
       uint32_t ms[W], ev[W], hw[W];
 #pragma unroll
       for (uint32_t j = 0; j < W; ++j) {
@@ -1029,10 +1027,6 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
 #pragma unroll
       for (uint32_t j = 0; j < W; ++j)
         ev[j] = ms[j] < E ? __ldg(base + (ms[j] >> 2) * 128u + (ms[j] & 3u)) : 0u;
-      if (first) {  // the unit's entries are no longer needed in registers
-        first = false;
-        if (u + nw < n) load_unit(u + nw);
-      }
 #pragma unroll
       for (uint32_t j = 0; j < W; ++j) hw[j] = ms[j] < E ? __ldg(hb + (ev[j] >> 5)) : 0u;
 #pragma unroll
@@ -1042,7 +1036,7 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
           pull_hit<BF16>(a, P, un.o0 + (ms[j] >> 2) * 128u + 4u * lane + (ms[j] & 3u), slot1);
         }
       }
-    } while (__any_sync(kFull, need != 0u));
+    }
   }
   hits = __reduce_add_sync(kFull, hits);
   if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
