@@ -193,7 +193,8 @@ struct StepArgs {
   uint32_t pull_sum;              // dense pulls: 0 every entry loads its history word; 1 entries
                                   // settle on a staged spike summary; 2 as 1, the per-step
                                   // kernel also staging its entry stream (k_pull_async); 3 as 1,
-                                  // the per-step kernel loading entries 16 bytes at a time
+                                  // the per-step kernel loading entries 16 bytes at a time; 4 as 3,
+                                  // passing entries queued and gathered in batches (k_pull_q)
   uint32_t any_push;
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer
@@ -232,6 +233,7 @@ cudaError_t pull_setup();
 int pull_blocks_per_sm(const StepArgs& a);
 size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summary rows
 size_t pull_async_smem_bytes(const StepArgs& a);  // k_pull_async: summary + entry buffers
+size_t pull_queue_smem_bytes(const StepArgs& a);  // k_pull_q: summary + per-warp queues
 size_t pair_stage_smem_bytes(const StepArgs& a);  // general kernel, lane_cells 3: dynamic smem
 size_t seg_smem_bytes(const StepArgs& a);  // shared memory of the segment descriptors
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).

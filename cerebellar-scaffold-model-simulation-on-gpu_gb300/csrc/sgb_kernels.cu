@@ -1042,6 +1042,109 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
   if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
 }
 
+// Dense pull, stream then gather (per-step driver; one 1,024-thread block per
+// SM).  Each warp streams its units' entries (16-byte loads as in
+// k_pull_vec) and only tests them against the staged summary; the offsets of
+// the few that pass go to the warp's queue in shared memory (up to kPullQueue,
+// one projection at a time).  A full queue, a change of projection or the end
+// of the warp's units drains it: every lane takes four queued offsets, re-reads
+// their entries (recently streamed: L1 / L2), loads their history words
+// together and adds the hits -- full lanes and four lookups in flight, instead
+// of one mostly idle walk per unit.  The next unit's loads are issued before a
+// drain, so they are in flight while it runs.
+constexpr uint32_t kPullQueue = 1024;  // offsets per warp queue (4 KiB)
+constexpr size_t kPullQueueBytes = (size_t)(kPullBlock / 32) * kPullQueue * 4;  // 128 KiB
+template <bool BF16>
+__global__ void __launch_bounds__(kPullBlock, 1) k_pull_q(StepArgs a) {
+  constexpr uint32_t V = kPullUnit / 128;  // 16-byte loads per lane per unit
+  extern __shared__ __align__(16) uint32_t s_sum[];  // [H][n_swords] + 1, then the queues
+  const size_t sum_words = ((size_t)a.hist_rows * a.n_swords + 1 + 3) & ~(size_t)3;
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  uint32_t* qo = s_sum + sum_words + (size_t)wib * kPullQueue;
+  const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
+  const uint32_t n = a.n_pull_units;
+  const StepIdx ix = step_of(a);
+  const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
+  uint4 q[V];
+  auto load_unit = [&](uint32_t u) {
+    const PullUnit un = a.pull_units[u];
+    const uint4* src = reinterpret_cast<const uint4*>(a.projs[un.proj].ell_syn + un.o0) + lane;
+#pragma unroll
+    for (uint32_t k = 0; k < V; ++k) q[k] = __ldg(src + 32u * k);
+  };
+  if (gw < n) load_unit(gw);
+  stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
+  __syncthreads();
+  const uint32_t* hb = hist_base(a, ix.hrow);
+  uint32_t hits = 0;
+  // Queue entries [0, cnt) of projection pj: four per lane per round.
+  auto drain = [&](uint32_t cnt, uint32_t pj) {
+    const ProjDev& P = a.projs[pj];
+    for (uint32_t b0 = 0; b0 < cnt; b0 += 128u) {
+      uint32_t o[4], e[4], hw[4];
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) {
+        const uint32_t i = b0 + 32u * k + lane;
+        o[k] = i < cnt ? qo[i] : 0xFFFFFFFFu;
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) e[k] = o[k] != 0xFFFFFFFFu ? __ldg(P.ell_syn + o[k]) : 0u;
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) hw[k] = o[k] != 0xFFFFFFFFu ? __ldg(hb + (e[k] >> 5)) : 0u;
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) {
+        if (o[k] != 0xFFFFFFFFu && ((hw[k] >> (e[k] & 31u)) & 1u)) {
+          ++hits;
+          pull_hit<BF16>(a, P, o[k], slot1);
+        }
+      }
+    }
+    __syncwarp();  // the queue is refilled after every lane has read it
+  };
+  uint32_t qn = 0, qproj = 0;  // warp-uniform
+  for (uint32_t u = gw; u < n; u += nw) {
+    const PullUnit un = a.pull_units[u];
+    uint32_t need = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < V; ++k) {
+      const uint32_t ev4[4] = {q[k].x, q[k].y, q[k].z, q[k].w};
+#pragma unroll
+      for (uint32_t j = 0; j < 4; ++j) {
+        const uint32_t sw = s_sum[ev4[j] >> 10];
+        need |= (__funnelshift_r(sw, sw, ev4[j] >> 5) & 1u) << (4u * k + j);
+      }
+    }
+    const uint32_t cnt = __popc(need);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(kFull, incl, o);
+      if (lane >= (uint32_t)o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    // The unit's entries are no longer needed in registers: the next unit's
+    // loads go out before any drain.
+    if (u + nw < n) load_unit(u + nw);
+    if (qn && (qn + total > kPullQueue || un.proj != qproj)) {
+      drain(qn, qproj);
+      qn = 0;
+    }
+    if (qn == 0) qproj = un.proj;
+    uint32_t pos = qn + incl - cnt;
+    while (need) {
+      const uint32_t m = __ffs(need) - 1u;
+      need &= need - 1u;
+      qo[pos++] = un.o0 + (m >> 2) * 128u + 4u * lane + (m & 3u);
+    }
+    qn += total;
+    __syncwarp();
+  }
+  if (qn) drain(qn, qproj);
+  hits = __reduce_add_sync(kFull, hits);
+  if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
+}
+
 // Dense pull with the entry stream staged in shared memory (per-step driver;
 // one 1,024-thread block per SM).  A warp takes half units (512 entries, 2 KB)
 // gw, gw + nw, ... and keeps two of them in flight: each lane copies 16-byte
@@ -2113,12 +2216,23 @@ size_t pair_stage_smem_bytes(const StepArgs& a) {
   return (a.seg_smem ? seg_smem_bytes_dev(a) : 0) + kPairStageBlockBytes;
 }
 
+// k_pull_q: the staged summary (rounded to 16 bytes) and the warps' queues.
+size_t pull_queue_smem_bytes(const StepArgs& a) {
+  return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + kPullQueueBytes;
+}
+
 size_t pull_async_smem_bytes(const StepArgs& a) {
   return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + kPullBufBytes;
 }
 
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
   if (!a.n_pull_units) return cudaSuccess;
+  if (a.pull_sum == 4u) {
+    const size_t smem = pull_queue_smem_bytes(a);
+    if (a.bf16) k_pull_q<true><<<blocks, kPullBlock, smem, s>>>(a);
+    else k_pull_q<false><<<blocks, kPullBlock, smem, s>>>(a);
+    return cudaGetLastError();
+  }
   if (a.pull_sum == 3u) {
     const size_t smem = pull_sum_bytes(a);
     if (a.bf16) k_pull_vec<true><<<blocks, kPullBlock, smem, s>>>(a);
@@ -2171,7 +2285,8 @@ cudaError_t pull_setup() {
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   // The opt-in limit covers static and dynamic shared memory together.
   for (const void* fn : {(const void*)k_persistent<true, true, 3>, (const void*)k_persistent<false, true, 3>,
-                         (const void*)k_pull_async<true>, (const void*)k_pull_async<false>}) {
+                         (const void*)k_pull_async<true>, (const void*)k_pull_async<false>,
+                         (const void*)k_pull_q<true>, (const void*)k_pull_q<false>}) {
     cudaFuncAttributes fa{};
     if ((e = cudaFuncGetAttributes(&fa, fn))) return e;
     const int lim = optin - (int)fa.sharedSizeBytes;

@@ -87,6 +87,25 @@ def _assert_same(counts, ids, offs, state, exp):
     assert np.array_equal(ref, eref)
 
 
+def test_config5x4_dense_pull_queue(tmp_path):
+    """Config 5 with 4 seeds (3.7M cells, 109M synapses), every projection
+    pulled densely by the per-step kernels with the queued gather (k_pull_q):
+    a spread of instances against their own oracle runs."""
+    seeds = [1, 2, 3, 4]
+    nets = [sg.scaffold(5, 1.0, sd) for sd in seeds]
+    steps = 60
+    sim = _with_shape(nets, seeds, [6, 2, 4, 0, 2],
+                      [sg.PROP_ELL] * sum(len(n.projections) for n in nets), sg.EXEC_GRAPH,
+                      tmp_path, weight_type=sg.WEIGHT_BF16, raster=True, chunk_steps=60)
+    assert sim.info().pull_summary == 4
+    counts, (ids, offs) = sim.loop_n_steps(steps, raster=True, raster_cap=1 << 22)
+    state = sim.state()
+    spikes = sum(_assert_instance(k, nets, seeds, counts, ids, offs, state, steps, True)
+                 for k in (0, 3))
+    assert spikes > 0 and sim.info().pulled > 0
+    sim.close()
+
+
 @pytest.mark.parametrize("weight", [sg.WEIGHT_FP32, sg.WEIGHT_BF16])
 @pytest.mark.parametrize("exec_mode", [sg.EXEC_PERSISTENT, sg.EXEC_GRAPH])
 def test_config2_dense_pull_in_degree_25000(weight, exec_mode):
