@@ -1174,9 +1174,9 @@ static TuneShape current_shape(const Sim& s) {
 static void apply_shape(Sim& s, const TuneShape& t) {
   s.args.item_log2 = (uint32_t)std::min(7, std::max(5, t.item_log2));
   s.deliver_blocks = std::min(8, std::max(1, t.deliver_mult)) * s.sm_count;
-  const bool ok = t.pull_sum == 0 || (s.pull_sum_fits && t.pull_sum >= 1 && t.pull_sum <= 4 &&
+  const bool ok = t.pull_sum == 0 || (s.pull_sum_fits && t.pull_sum >= 1 && t.pull_sum <= 5 &&
                                       (t.pull_sum != 2 || s.pull_async_fits) &&
-                                      (t.pull_sum != 4 || s.pull_queue_fits));
+                                      (t.pull_sum < 4 || s.pull_queue_fits));
   s.args.pull_sum = ok ? (uint32_t)t.pull_sum : (s.pull_sum_fits ? 1u : 0u);
   s.args.ahead = t.ahead ? 1u : 0u;
   s.args.lane_cells = t.lane_cells == 3 && s.pair_stage_fits ? 3u : (t.lane_cells >= 2 ? 2u : 1u);
@@ -1351,9 +1351,9 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
       for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead, cur.lane_cells});
     // The other dense-pull variants: no summary; summary; summary with staged
     // entries (per-step kernel); summary with 16-byte entry loads (per-step).
-    for (int32_t ps = 0; s.args.n_pull_units && ps <= 4; ++ps) {
+    for (int32_t ps = 0; s.args.n_pull_units && ps <= 5; ++ps) {
       const bool ok = ps == 0 || (s.pull_sum_fits && (ps != 2 || s.pull_async_fits) &&
-                                  (ps != 4 || s.pull_queue_fits));
+                                  (ps < 4 || s.pull_queue_fits));
       if (ok && ps != cur.pull_sum && (ps < 2 || !persistent)) cands.push_back({-1 - ps, -1, -1, -1, -1});
     }
     for (TuneShape c : cands) {

@@ -1045,22 +1045,23 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
 // Dense pull, stream then gather (per-step driver; one 1,024-thread block per
 // SM).  Each warp streams its units' entries (16-byte loads as in
 // k_pull_vec) and only tests them against the staged summary; the offsets of
-// the few that pass go to the warp's queue in shared memory (up to kPullQueue,
+// the few that pass go to the warp's queue in shared memory (QCAP offsets,
 // one projection at a time).  A full queue, a change of projection or the end
 // of the warp's units drains it: every lane takes four queued offsets, re-reads
 // their entries (recently streamed: L1 / L2), loads their history words
 // together and adds the hits -- full lanes and four lookups in flight, instead
 // of one mostly idle walk per unit.  The next unit's loads are issued before a
 // drain, so they are in flight while it runs.
-constexpr uint32_t kPullQueue = 1024;  // offsets per warp queue (4 KiB)
-constexpr size_t kPullQueueBytes = (size_t)(kPullBlock / 32) * kPullQueue * 4;  // 128 KiB
-template <bool BF16>
+constexpr uint32_t kPullQueueA = 256, kPullQueueB = 128;  // offsets per warp queue
+// QCAP: offsets per warp queue (a unit may pass more: it is then queued in
+// parts, the queue drained between them).
+template <bool BF16, uint32_t QCAP>
 __global__ void __launch_bounds__(kPullBlock, 1) k_pull_q(StepArgs a) {
   constexpr uint32_t V = kPullUnit / 128;  // 16-byte loads per lane per unit
   extern __shared__ __align__(16) uint32_t s_sum[];  // [H][n_swords] + 1, then the queues
   const size_t sum_words = ((size_t)a.hist_rows * a.n_swords + 1 + 3) & ~(size_t)3;
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-  uint32_t* qo = s_sum + sum_words + (size_t)wib * kPullQueue;
+  uint32_t* qo = s_sum + sum_words + (size_t)wib * QCAP;
   const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
   const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
   const uint32_t n = a.n_pull_units;
@@ -1126,19 +1127,33 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_q(StepArgs a) {
     // The unit's entries are no longer needed in registers: the next unit's
     // loads go out before any drain.
     if (u + nw < n) load_unit(u + nw);
-    if (qn && (qn + total > kPullQueue || un.proj != qproj)) {
+    if (qn && (qn + total > QCAP || un.proj != qproj)) {
       drain(qn, qproj);
       qn = 0;
     }
-    if (qn == 0) qproj = un.proj;
-    uint32_t pos = qn + incl - cnt;
-    while (need) {
-      const uint32_t m = __ffs(need) - 1u;
-      need &= need - 1u;
-      qo[pos++] = un.o0 + (m >> 2) * 128u + 4u * lane + (m & 3u);
+    qproj = un.proj;
+    // Lane offsets in the unit's queued run; a run longer than the queue is
+    // queued and drained in parts of QCAP.
+    uint32_t pos = incl - cnt;
+    for (uint32_t part = 0; part < total; part += QCAP) {
+      uint32_t nd = need;
+      uint32_t p2 = pos;
+      while (nd) {
+        const uint32_t m = __ffs(nd) - 1u;
+        nd &= nd - 1u;
+        if (p2 >= part && p2 < part + QCAP)
+          qo[qn + p2 - part] = un.o0 + (m >> 2) * 128u + 4u * lane + (m & 3u);
+        ++p2;
+      }
+      __syncwarp();
+      const uint32_t got = min(QCAP, total - part);
+      if (part + QCAP < total) {  // a full part: gather it now
+        drain(qn + got, qproj);
+        qn = 0;
+      } else {
+        qn += got;
+      }
     }
-    qn += total;
-    __syncwarp();
   }
   if (qn) drain(qn, qproj);
   hits = __reduce_add_sync(kFull, hits);
@@ -2218,7 +2233,7 @@ size_t pair_stage_smem_bytes(const StepArgs& a) {
 
 // k_pull_q: the staged summary (rounded to 16 bytes) and the warps' queues.
 size_t pull_queue_smem_bytes(const StepArgs& a) {
-  return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + kPullQueueBytes;
+  return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + (size_t)(kPullBlock / 32) * kPullQueueA * 4;
 }
 
 size_t pull_async_smem_bytes(const StepArgs& a) {
@@ -2227,10 +2242,15 @@ size_t pull_async_smem_bytes(const StepArgs& a) {
 
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
   if (!a.n_pull_units) return cudaSuccess;
-  if (a.pull_sum == 4u) {
+  if (a.pull_sum == 4u || a.pull_sum == 5u) {
     const size_t smem = pull_queue_smem_bytes(a);
-    if (a.bf16) k_pull_q<true><<<blocks, kPullBlock, smem, s>>>(a);
-    else k_pull_q<false><<<blocks, kPullBlock, smem, s>>>(a);
+    if (a.pull_sum == 4u) {
+      if (a.bf16) k_pull_q<true, kPullQueueA><<<blocks, kPullBlock, smem, s>>>(a);
+      else k_pull_q<false, kPullQueueA><<<blocks, kPullBlock, smem, s>>>(a);
+    } else {
+      if (a.bf16) k_pull_q<true, kPullQueueB><<<blocks, kPullBlock, smem, s>>>(a);
+      else k_pull_q<false, kPullQueueB><<<blocks, kPullBlock, smem, s>>>(a);
+    }
     return cudaGetLastError();
   }
   if (a.pull_sum == 3u) {
@@ -2286,7 +2306,8 @@ cudaError_t pull_setup() {
   // The opt-in limit covers static and dynamic shared memory together.
   for (const void* fn : {(const void*)k_persistent<true, true, 3>, (const void*)k_persistent<false, true, 3>,
                          (const void*)k_pull_async<true>, (const void*)k_pull_async<false>,
-                         (const void*)k_pull_q<true>, (const void*)k_pull_q<false>}) {
+                         (const void*)k_pull_q<true, kPullQueueA>, (const void*)k_pull_q<false, kPullQueueA>,
+                         (const void*)k_pull_q<true, kPullQueueB>, (const void*)k_pull_q<false, kPullQueueB>}) {
     cudaFuncAttributes fa{};
     if ((e = cudaFuncGetAttributes(&fa, fn))) return e;
     const int lim = optin - (int)fa.sharedSizeBytes;

@@ -351,6 +351,7 @@ def test_general_kernel_block_item_overflow(delay):
     (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 3, 0]),       # k_pull_vec: 16-byte entry loads
     (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 4, 0]),       # k_pull_q: passing entries queued, gathered
     (sg.EXEC_GRAPH, None, [6, 2, 4, 0]),              # k_pull_q with pushes beside it
+    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 5, 0]),       # k_pull_q, 128-offset queues
     (sg.EXEC_PERSISTENT, sg.PROP_ELL, [6, 4, 0, 1]),  # resident kernel, pulls without the summary
 ])
 def test_cached_launch_shapes_bit_exact(tmp_path, exec_mode, prop, shape):
