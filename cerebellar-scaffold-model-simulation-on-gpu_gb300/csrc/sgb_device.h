@@ -182,8 +182,7 @@ struct StepArgs {
   uint32_t max_delay;             // longest synaptic delay, steps (ring_slots = max_delay + 2)
   uint32_t item_log2;             // fused persistent kernel: push items of 2^item_log2 synapses
   uint32_t ahead;                 // fused persistent kernel: spike-ahead timeline (one substep)
-  uint32_t lane_cells;            // general persistent kernel, one-barrier form: 1 or 2 cells per
-                                  // lane, 3 two cells with the loads staged in shared memory
+  uint32_t lane_cells;            // general persistent kernel, one-barrier form: cells per lane (1, 2)
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
   uint32_t stdp_early;            // every plastic rule reads only earlier steps' spikes (Teacher)
@@ -192,9 +191,7 @@ struct StepArgs {
   uint32_t n_swords;              // summary words per row: ceil(n_words / 32)
   uint32_t pull_sum;              // dense pulls: 0 every entry loads its history word; 1 entries
                                   // settle on a staged spike summary; 2 as 1, the per-step
-                                  // kernel also staging its entry stream (k_pull_async); 3 as 1,
-                                  // the per-step kernel loading entries 16 bytes at a time; 4 as 3,
-                                  // passing entries queued and gathered in batches (k_pull_q)
+                                  // kernel loading entries 16 bytes at a time (k_pull_vec)
   uint32_t any_push;
   uint32_t raster_cap;
   uint32_t item_cap;              // items per parity buffer
@@ -232,9 +229,6 @@ cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s);
 cudaError_t pull_setup();
 int pull_blocks_per_sm(const StepArgs& a);
 size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summary rows
-size_t pull_async_smem_bytes(const StepArgs& a);  // k_pull_async: summary + entry buffers
-size_t pull_queue_smem_bytes(const StepArgs& a);  // k_pull_q: summary + per-warp queues
-size_t pair_stage_smem_bytes(const StepArgs& a);  // general kernel, lane_cells 3: dynamic smem
 size_t seg_smem_bytes(const StepArgs& a);  // shared memory of the segment descriptors
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
 int persistent_kernel_kind(const StepArgs& a, int blocks);

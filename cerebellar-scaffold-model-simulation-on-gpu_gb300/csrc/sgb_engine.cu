@@ -652,15 +652,7 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   // per-step pull kernel may also stage its entry stream (the autotuner's
   // choice, where that fits too).
   s.pull_sum_fits = a.pull_sum != 0;
-  if (a.pull_sum) a.pull_sum = 3u;  // summary staged; the per-step pull loads entries 16 B at a time
-  {
-    int optin = 0;
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device);
-    s.pull_async_fits = a.pull_sum && pull_async_smem_bytes(a) <= (size_t)optin;
-    s.pull_queue_fits = a.pull_sum && pull_queue_smem_bytes(a) <= (size_t)optin;
-    // (with room for the kernel's 8.5 KB of static shared memory)
-    s.pair_stage_fits = pair_stage_smem_bytes(a) + 16384 <= (size_t)optin;
-  }
+  if (a.pull_sum) a.pull_sum = 2u;  // summary staged; the per-step pull loads entries 16 B at a time
   // The cell state is read and rewritten every step; where the device lets
   // this context set L2 aside for persisting accesses, the state window
   // stays in L2 across steps while ring slots, tables and history stream
@@ -1159,7 +1151,7 @@ static std::string tune_signature(const Sim& s) {
 struct TuneShape {
   int32_t item_log2;     // fused kernel: push items of 2^item_log2 synapses
   int32_t deliver_mult;  // per-step driver: delivery blocks per SM
-  int32_t pull_sum;      // dense pulls: 0 no summary, 1 staged summary, 2 also staged entries
+  int32_t pull_sum;      // dense pulls: 0 no summary, 1 staged summary, 2 also 16-byte entry loads
   int32_t ahead;         // fused kernel: 1 spike-ahead timeline, 0 spikes in their own step
   int32_t lane_cells;    // general kernel's one-barrier form: cells per lane (1 or 2)
 };
@@ -1174,12 +1166,10 @@ static TuneShape current_shape(const Sim& s) {
 static void apply_shape(Sim& s, const TuneShape& t) {
   s.args.item_log2 = (uint32_t)std::min(7, std::max(5, t.item_log2));
   s.deliver_blocks = std::min(8, std::max(1, t.deliver_mult)) * s.sm_count;
-  const bool ok = t.pull_sum == 0 || (s.pull_sum_fits && t.pull_sum >= 1 && t.pull_sum <= 5 &&
-                                      (t.pull_sum != 2 || s.pull_async_fits) &&
-                                      (t.pull_sum < 4 || s.pull_queue_fits));
-  s.args.pull_sum = ok ? (uint32_t)t.pull_sum : (s.pull_sum_fits ? 1u : 0u);
+  const bool ok = t.pull_sum == 0 || (s.pull_sum_fits && t.pull_sum >= 1 && t.pull_sum <= 2);
+  s.args.pull_sum = ok ? (uint32_t)t.pull_sum : (s.pull_sum_fits ? 2u : 0u);
   s.args.ahead = t.ahead ? 1u : 0u;
-  s.args.lane_cells = t.lane_cells == 3 && s.pair_stage_fits ? 3u : (t.lane_cells >= 2 ? 2u : 1u);
+  s.args.lane_cells = t.lane_cells >= 2 ? 2u : 1u;
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
 }
@@ -1344,16 +1334,14 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
     }
     if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_GENERAL &&
         general_one_barrier(s.args) && s.args.n_plast == 0)
-      for (int32_t lc = 1; lc <= (s.pair_stage_fits ? 3 : 2); ++lc)  // cells per lane, staging
-        if (lc != cur.lane_cells)
-          cands.push_back({cur.item_log2, cur.deliver_mult, cur.pull_sum, cur.ahead, lc});
+      cands.push_back({cur.item_log2, cur.deliver_mult, cur.pull_sum, cur.ahead,
+                       3 - cur.lane_cells});  // one or two cells per lane
     if (!persistent)
       for (int32_t m : {1, 4}) cands.push_back({cur.item_log2, m, cur.pull_sum, cur.ahead, cur.lane_cells});
-    // The other dense-pull variants: no summary; summary; summary with staged
-    // entries (per-step kernel); summary with 16-byte entry loads (per-step).
-    for (int32_t ps = 0; s.args.n_pull_units && ps <= 5; ++ps) {
-      const bool ok = ps == 0 || (s.pull_sum_fits && (ps != 2 || s.pull_async_fits) &&
-                                  (ps < 4 || s.pull_queue_fits));
+    // The other dense-pull variants: no summary; summary; summary with
+    // 16-byte entry loads (the per-step kernel; the persistent kernels treat 2 as 1).
+    for (int32_t ps = 0; s.args.n_pull_units && ps <= 2; ++ps) {
+      const bool ok = ps == 0 || s.pull_sum_fits;
       if (ok && ps != cur.pull_sum && (ps < 2 || !persistent)) cands.push_back({-1 - ps, -1, -1, -1, -1});
     }
     for (TuneShape c : cands) {

@@ -48,9 +48,6 @@ struct Sim {
   std::vector<SrcDev> srcs;
   std::vector<int32_t> src_net, src_idx;
   bool pull_sum_fits = false;    // the staged spike summary fits shared memory
-  bool pull_async_fits = false;  // ... and k_pull_async's entry buffers beside it
-  bool pull_queue_fits = false;  // ... and k_pull_q's queues beside it
-  bool pair_stage_fits = false;  // the general kernel's staged pairs fit shared memory
   uint32_t n_pad = 0, n_words = 0, ring_slots = 3, hist_rows = 1, max_delay = 1;
   int64_t n_cells = 0, n_syn = 0;
   uint32_t chunk = 1000, raster_cap = 0;

@@ -16,9 +16,7 @@
 //            (the reference's pull, Simulation_header.cu:83-139, with the delay
 //            applied on read as at GPUScaffoldSimulation.cu:735).
 // Two drivers run these phases: per-step kernels (replayed from a CUDA graph;
-// kernel boundaries order the phases; the dense pull streams its entries
-// through shared memory with asynchronous copies, two half units in flight
-// per warp, where they fit) and one persistent cooperative kernel
+// kernel boundaries order the phases) and one persistent cooperative kernel
 // per chunk of steps (a bounded grid barrier orders them).  The persistent
 // kernel comes in three forms: fused (every word resident in one warp, every
 // projection event-driven: update and push share one phase, one barrier a
@@ -594,61 +592,6 @@ __device__ __forceinline__ uint32_t update_pairs(const StepArgs& a, uint32_t gp,
   return walked;
 }
 
-// Staged pairs (lane_cells 3): a warp's next kPairStages pairs stream into its
-// shared-memory stages with 16-byte cp.async.cg copies (at L2: ring slots and
-// state are rewritten by other SMs during the launch) -- ring entries (512 B),
-// conductances (512 B) and potentials (256 B) per pair -- so three pairs are
-// in flight per warp without holding registers for them.
-constexpr uint32_t kPairStages = 3;
-constexpr uint32_t kPairStageBytes = 1280;
-constexpr size_t kPairStageBlockBytes = (size_t)(kPersistBlock / 32) * kPairStages * kPairStageBytes;
-
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-
-template <bool SEGSMEM, bool BF16>
-__device__ __forceinline__ uint32_t update_pairs_staged(const StepArgs& a, uint32_t gp, uint32_t np,
-                                                        const StepIdx& ix, BlockItems bi,
-                                                        unsigned char* stages) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t n_pairs = a.n_words >> 1;
-  const unsigned char* my = stages + (size_t)(threadIdx.x >> 5) * kPairStages * kPairStageBytes;
-  const uint32_t my_s = (uint32_t)__cvta_generic_to_shared(my);
-  // Pair p into stage k: lane L copies its two cells' ring entries and
-  // conductances; lanes 0..15 copy four cells' potentials each.
-  auto issue = [&](uint32_t p, uint32_t k) {
-    if (p < n_pairs) {
-      const uint32_t c = p << 6;
-      const uint32_t d = my_s + k * kPairStageBytes;
-      cp_async16(d + 16u * lane, reinterpret_cast<const int2*>(a.ring) + (ix.roff + c + 2u * lane));
-      cp_async16(d + 512u + 16u * lane, a.sg + c + 2u * lane);
-      if (lane < 16u) cp_async16(d + 1024u + 16u * lane, a.su + c + 4u * lane);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
-  issue(gp, 0u);
-  issue(gp + np, 1u);
-  issue(gp + 2u * np, 2u);
-  uint32_t walked = 0, k = 0;
-  for (uint32_t p = gp; p < n_pairs; p += np) {
-    asm volatile("cp.async.wait_group 2;" ::: "memory");  // the oldest group is pair p's
-    __syncwarp();
-    const unsigned char* st = my + k * kPairStageBytes;
-    PairIn in;
-    in.acc = *reinterpret_cast<const int4*>(st + 16u * lane);
-    in.g = *reinterpret_cast<const float4*>(st + 512u + 16u * lane);
-    in.u = *reinterpret_cast<const float2*>(st + 1024u + 8u * lane);
-    in.seg = __ldg(a.seg_of_word + (((p << 6) + 2u * lane) >> 5));
-    __syncwarp();  // every lane has read the stage before it is refilled
-    issue(p + 3u * np, k);
-    walked += finish_pair<SEGSMEM, BF16>(a, p, in, ix, bi);
-    k = k + 1u == kPairStages ? 0u : k + 1u;
-  }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  return walked;
-}
-
 // ---- phase 2: deliveries ------------------------------------------------------
 // One warp delivers one push item (at most kPushChunk synapses of a spiking
 // cell's row): all loads of the item are issued before its atomics so the
@@ -1042,212 +985,6 @@ __global__ void __launch_bounds__(kPullBlock, 1) k_pull_vec(StepArgs a) {
   if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
 }
 
-// Dense pull, stream then gather (per-step driver; one 1,024-thread block per
-// SM).  Each warp streams its units' entries (16-byte loads as in
-// k_pull_vec) and only tests them against the staged summary; the offsets of
-// the few that pass go to the warp's queue in shared memory (QCAP offsets,
-// one projection at a time).  A full queue, a change of projection or the end
-// of the warp's units drains it: every lane takes four queued offsets, re-reads
-// their entries (recently streamed: L1 / L2), loads their history words
-// together and adds the hits -- full lanes and four lookups in flight, instead
-// of one mostly idle walk per unit.  The next unit's loads are issued before a
-// drain, so they are in flight while it runs.
-constexpr uint32_t kPullQueueA = 256, kPullQueueB = 128;  // offsets per warp queue
-// QCAP: offsets per warp queue (a unit may pass more: it is then queued in
-// parts, the queue drained between them).
-template <bool BF16, uint32_t QCAP>
-__global__ void __launch_bounds__(kPullBlock, 1) k_pull_q(StepArgs a) {
-  constexpr uint32_t V = kPullUnit / 128;  // 16-byte loads per lane per unit
-  extern __shared__ __align__(16) uint32_t s_sum[];  // [H][n_swords] + 1, then the queues
-  const size_t sum_words = ((size_t)a.hist_rows * a.n_swords + 1 + 3) & ~(size_t)3;
-  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-  uint32_t* qo = s_sum + sum_words + (size_t)wib * QCAP;
-  const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
-  const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
-  const uint32_t n = a.n_pull_units;
-  const StepIdx ix = step_of(a);
-  const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
-  uint4 q[V];
-  auto load_unit = [&](uint32_t u) {
-    const PullUnit un = a.pull_units[u];
-    const uint4* src = reinterpret_cast<const uint4*>(a.projs[un.proj].ell_syn + un.o0) + lane;
-#pragma unroll
-    for (uint32_t k = 0; k < V; ++k) q[k] = __ldg(src + 32u * k);
-  };
-  if (gw < n) load_unit(gw);
-  stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
-  __syncthreads();
-  const uint32_t* hb = hist_base(a, ix.hrow);
-  uint32_t hits = 0;
-  // Queue entries [0, cnt) of projection pj: four per lane per round.
-  auto drain = [&](uint32_t cnt, uint32_t pj) {
-    const ProjDev& P = a.projs[pj];
-    for (uint32_t b0 = 0; b0 < cnt; b0 += 128u) {
-      uint32_t o[4], e[4], hw[4];
-#pragma unroll
-      for (uint32_t k = 0; k < 4; ++k) {
-        const uint32_t i = b0 + 32u * k + lane;
-        o[k] = i < cnt ? qo[i] : 0xFFFFFFFFu;
-      }
-#pragma unroll
-      for (uint32_t k = 0; k < 4; ++k) e[k] = o[k] != 0xFFFFFFFFu ? __ldg(P.ell_syn + o[k]) : 0u;
-#pragma unroll
-      for (uint32_t k = 0; k < 4; ++k) hw[k] = o[k] != 0xFFFFFFFFu ? __ldg(hb + (e[k] >> 5)) : 0u;
-#pragma unroll
-      for (uint32_t k = 0; k < 4; ++k) {
-        if (o[k] != 0xFFFFFFFFu && ((hw[k] >> (e[k] & 31u)) & 1u)) {
-          ++hits;
-          pull_hit<BF16>(a, P, o[k], slot1);
-        }
-      }
-    }
-    __syncwarp();  // the queue is refilled after every lane has read it
-  };
-  uint32_t qn = 0, qproj = 0;  // warp-uniform
-  for (uint32_t u = gw; u < n; u += nw) {
-    const PullUnit un = a.pull_units[u];
-    uint32_t need = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < V; ++k) {
-      const uint32_t ev4[4] = {q[k].x, q[k].y, q[k].z, q[k].w};
-#pragma unroll
-      for (uint32_t j = 0; j < 4; ++j) {
-        const uint32_t sw = s_sum[ev4[j] >> 10];
-        need |= (__funnelshift_r(sw, sw, ev4[j] >> 5) & 1u) << (4u * k + j);
-      }
-    }
-    const uint32_t cnt = __popc(need);
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t v = __shfl_up_sync(kFull, incl, o);
-      if (lane >= (uint32_t)o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(kFull, incl, 31);
-    // The unit's entries are no longer needed in registers: the next unit's
-    // loads go out before any drain.
-    if (u + nw < n) load_unit(u + nw);
-    if (qn && (qn + total > QCAP || un.proj != qproj)) {
-      drain(qn, qproj);
-      qn = 0;
-    }
-    qproj = un.proj;
-    // Lane offsets in the unit's queued run; a run longer than the queue is
-    // queued and drained in parts of QCAP.
-    uint32_t pos = incl - cnt;
-    for (uint32_t part = 0; part < total; part += QCAP) {
-      uint32_t nd = need;
-      uint32_t p2 = pos;
-      while (nd) {
-        const uint32_t m = __ffs(nd) - 1u;
-        nd &= nd - 1u;
-        if (p2 >= part && p2 < part + QCAP)
-          qo[qn + p2 - part] = un.o0 + (m >> 2) * 128u + 4u * lane + (m & 3u);
-        ++p2;
-      }
-      __syncwarp();
-      const uint32_t got = min(QCAP, total - part);
-      if (part + QCAP < total) {  // a full part: gather it now
-        drain(qn + got, qproj);
-        qn = 0;
-      } else {
-        qn += got;
-      }
-    }
-  }
-  if (qn) drain(qn, qproj);
-  hits = __reduce_add_sync(kFull, hits);
-  if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
-}
-
-// Dense pull with the entry stream staged in shared memory (per-step driver;
-// one 1,024-thread block per SM).  A warp takes half units (512 entries, 2 KB)
-// gw, gw + nw, ... and keeps two of them in flight: each lane copies 16-byte
-// chunks of a half unit into the warp's shared-memory buffer with cp.async.cg
-// (at L2, no registers held), and while one buffer is settled the other one
-// loads.  Settling reads the entries from shared memory: the summary test
-// (s_sum, staged as in k_pull) passes few of them, the passing ones load their
-// history word (four at a time) and the hits add their weight into the ring.
-// Shared memory: the staged summary, then 2 x 2 KB per warp.
-constexpr uint32_t kHalfUnit = kPullUnit / 2;
-constexpr size_t kPullBufBytes = (size_t)(kPullBlock / 32) * 2 * kHalfUnit * 4;  // 128 KiB
-template <bool BF16>
-__global__ void __launch_bounds__(kPullBlock, 1) k_pull_async(StepArgs a) {
-  constexpr uint32_t E = kHalfUnit / 32;  // entries per lane per half unit
-  constexpr uint32_t W = 4;               // history words loaded per trip
-  extern __shared__ __align__(16) uint32_t s_sum[];  // [H][n_swords] + 1, then the buffers
-  const size_t sum_words = ((size_t)a.hist_rows * a.n_swords + 1 + 3) & ~(size_t)3;
-  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-  uint32_t* buf = s_sum + sum_words + (size_t)wib * 2u * kHalfUnit;
-  const uint32_t gw = (blockIdx.x * kPullBlock + threadIdx.x) >> 5;
-  const uint32_t nw = (gridDim.x * kPullBlock) >> 5;
-  const uint32_t n = 2u * a.n_pull_units;  // half units
-  const StepIdx ix = step_of(a);
-  const uint32_t slot1 = ix.slot + 1u == a.ring_slots ? 0u : ix.slot + 1u;
-  // Copies half unit v into buffer b (lane: chunks lane, lane + 32, ...).
-  auto issue = [&](uint32_t v, uint32_t b) {
-    if (v < n) {
-      const PullUnit un = a.pull_units[v >> 1];
-      const uint32_t* src = a.projs[un.proj].ell_syn + un.o0 + (v & 1u) * kHalfUnit;
-      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(buf + b * kHalfUnit);
-#pragma unroll
-      for (uint32_t c = 0; c < kHalfUnit / 4 / 32; ++c) {
-        const uint32_t k = c * 32u + lane;  // 16-byte chunk index
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst + k * 16u),
-                     "l"(src + k * 4u) : "memory");
-      }
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  };
-  issue(gw, 0u);
-  issue(gw + nw, 1u);
-  stage_summary(a, ix, s_sum, threadIdx.x, kPullBlock);
-  __syncthreads();
-  const uint32_t* hb = hist_base(a, ix.hrow);
-  uint32_t hits = 0;
-  uint32_t b = 0;
-  for (uint32_t v = gw; v < n; v += nw, b ^= 1u) {
-    // The older of the two groups in flight is this buffer's.
-    asm volatile("cp.async.wait_group 1;" ::: "memory");
-    __syncwarp();
-    const uint32_t* e = buf + b * kHalfUnit;
-    const PullUnit un = a.pull_units[v >> 1];
-    const ProjDev& P = a.projs[un.proj];
-    const uint32_t o0 = un.o0 + (v & 1u) * kHalfUnit;
-    uint32_t need = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < E; ++k) {
-      const uint32_t ek = e[k * 32u + lane];
-      const uint32_t sw = s_sum[ek >> 10];
-      need |= (__funnelshift_r(sw, sw, ek >> 5) & 1u) << k;
-    }
-    while (need) {
-      uint32_t ks[W], ev[W], hw[W];
-#pragma unroll
-      for (uint32_t j = 0; j < W; ++j) {
-        ks[j] = need ? __ffs(need) - 1u : E;
-        need &= need - 1u;
-      }
-#pragma unroll
-      for (uint32_t j = 0; j < W; ++j) ev[j] = ks[j] < E ? e[ks[j] * 32u + lane] : 0u;
-#pragma unroll
-      for (uint32_t j = 0; j < W; ++j) hw[j] = ks[j] < E ? __ldg(hb + (ev[j] >> 5)) : 0u;
-#pragma unroll
-      for (uint32_t j = 0; j < W; ++j) {
-        if (ks[j] < E && ((hw[j] >> (ev[j] & 31u)) & 1u)) {
-          ++hits;
-          pull_hit<BF16>(a, P, o0 + ks[j] * 32u + lane, slot1);
-        }
-      }
-    }
-    __syncwarp();  // every lane is done with this buffer
-    issue(v + 2u * nw, b);
-  }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  hits = __reduce_add_sync(kFull, hits);
-  if (lane == 0 && hits) atomicAdd(&a.ctl->pulled, (unsigned long long)hits);
-}
-
 // STDP of the plastic projections, step t (SynapticPlasticity.cu:40-120), run
 // after the cells of step t updated and before the dense pull that delivers
 // into slot t + 1, so that delivery uses the new values -- in the reference
@@ -1563,15 +1300,12 @@ __device__ void raster_offsets_from_counts(const StepArgs& a, uint32_t n_steps, 
 // right after it, and one grid barrier ends the step.  Otherwise the items go
 // to a global list delivered by all warps between two grid barriers.
 // LANE (one-barrier form, no plasticity): 1 one cell per lane (update_words),
-// 2 two cells per lane (update_pairs), 3 two cells per lane with the loads
-// staged in shared memory (update_pairs_staged).
+// 2 two cells per lane (update_pairs).
 template <bool BF16, bool ONE, int LANE = 1>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uint32_t n_steps) {
   // Dynamic shared memory: the segment descriptors every word reads (when
   // a.seg_smem), then the staged spike summary (dense pulls, when it fits).
   uint32_t* s_sum = reinterpret_cast<uint32_t*>(g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0));
-  // LANE 3: the warps' pair stages after the segment descriptors.
-  unsigned char* pair_stages = g_dyn + (a.seg_smem ? seg_smem_bytes_dev(a) : 0);
   __shared__ uint2 s_items[ONE ? kGenItems : 1];
   __shared__ uint32_t s_icnt[2];  // item count of step parity p; the other one is reset
   __shared__ uint32_t s_wsum[kPersistBlock / 32];
@@ -1615,9 +1349,6 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent(StepArgs a, uin
     else if (LANE == 2)
       walked += a.seg_smem ? update_pairs<true, BF16>(a, uw, nw, ix, bi)
                            : update_pairs<false, BF16>(a, uw, nw, ix, bi);
-    else if (LANE == 3)
-      walked += a.seg_smem ? update_pairs_staged<true, BF16>(a, uw, nw, ix, bi, pair_stages)
-                           : update_pairs_staged<false, BF16>(a, uw, nw, ix, bi, pair_stages);
     else
       walked += a.seg_smem ? update_words<false, true, BF16, ONE>(a, uw, nw, ix, bi)
                            : update_words<false, false, BF16, ONE>(a, uw, nw, ix, bi);
@@ -2225,44 +1956,12 @@ size_t seg_smem_bytes(const StepArgs& a) { return seg_smem_bytes_dev(a); }
 
 static size_t pull_smem_bytes(const StepArgs& a) { return a.pull_sum ? pull_sum_bytes(a) : 0; }
 
-// k_pull_async: the staged summary (rounded to 16 bytes) and the warps' buffers.
-// The general kernel's staged pairs: descriptors and the warps' stages.
-size_t pair_stage_smem_bytes(const StepArgs& a) {
-  return (a.seg_smem ? seg_smem_bytes_dev(a) : 0) + kPairStageBlockBytes;
-}
-
-// k_pull_q: the staged summary (rounded to 16 bytes) and the warps' queues.
-size_t pull_queue_smem_bytes(const StepArgs& a) {
-  return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + (size_t)(kPullBlock / 32) * kPullQueueA * 4;
-}
-
-size_t pull_async_smem_bytes(const StepArgs& a) {
-  return ((pull_sum_bytes(a) + 15) & ~(size_t)15) + kPullBufBytes;
-}
-
 cudaError_t launch_pull(const StepArgs& a, int blocks, cudaStream_t s) {
   if (!a.n_pull_units) return cudaSuccess;
-  if (a.pull_sum == 4u || a.pull_sum == 5u) {
-    const size_t smem = pull_queue_smem_bytes(a);
-    if (a.pull_sum == 4u) {
-      if (a.bf16) k_pull_q<true, kPullQueueA><<<blocks, kPullBlock, smem, s>>>(a);
-      else k_pull_q<false, kPullQueueA><<<blocks, kPullBlock, smem, s>>>(a);
-    } else {
-      if (a.bf16) k_pull_q<true, kPullQueueB><<<blocks, kPullBlock, smem, s>>>(a);
-      else k_pull_q<false, kPullQueueB><<<blocks, kPullBlock, smem, s>>>(a);
-    }
-    return cudaGetLastError();
-  }
-  if (a.pull_sum == 3u) {
+  if (a.pull_sum == 2u) {
     const size_t smem = pull_sum_bytes(a);
     if (a.bf16) k_pull_vec<true><<<blocks, kPullBlock, smem, s>>>(a);
     else k_pull_vec<false><<<blocks, kPullBlock, smem, s>>>(a);
-    return cudaGetLastError();
-  }
-  if (a.pull_sum == 2u) {
-    const size_t smem = pull_async_smem_bytes(a);
-    if (a.bf16) k_pull_async<true><<<blocks, kPullBlock, smem, s>>>(a);
-    else k_pull_async<false><<<blocks, kPullBlock, smem, s>>>(a);
     return cudaGetLastError();
   }
   const size_t smem = pull_smem_bytes(a);
@@ -2300,19 +1999,6 @@ cudaError_t launch_plast_reset(const StepArgs& a, int blocks, cudaStream_t s) {
 cudaError_t pull_setup() {
   const int mx = (int)kPullSumMax;
   cudaError_t e;
-  int dev = 0, optin = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  // The opt-in limit covers static and dynamic shared memory together.
-  for (const void* fn : {(const void*)k_persistent<true, true, 3>, (const void*)k_persistent<false, true, 3>,
-                         (const void*)k_pull_async<true>, (const void*)k_pull_async<false>,
-                         (const void*)k_pull_q<true, kPullQueueA>, (const void*)k_pull_q<false, kPullQueueA>,
-                         (const void*)k_pull_q<true, kPullQueueB>, (const void*)k_pull_q<false, kPullQueueB>}) {
-    cudaFuncAttributes fa{};
-    if ((e = cudaFuncGetAttributes(&fa, fn))) return e;
-    const int lim = optin - (int)fa.sharedSizeBytes;
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, lim))) return e;
-  }
   if ((e = cudaFuncSetAttribute(k_pull_vec<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
   if ((e = cudaFuncSetAttribute(k_pull_vec<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx))) return e;
 
@@ -2417,21 +2103,16 @@ cudaError_t launch_persistent(const StepArgs& a, uint32_t n_steps, int blocks, c
                    : resident ? (a.bf16 ? (const void*)k_persistent_resident<true>
                                         : (const void*)k_persistent_resident<false>)
                    : general_one_barrier(a)
-                       ? (a.n_plast == 0 && a.lane_cells == 3u
-                              ? (a.bf16 ? (const void*)k_persistent<true, true, 3>
-                                        : (const void*)k_persistent<false, true, 3>)
-                          : a.n_plast == 0 && a.lane_cells == 2u
+                       ? (a.n_plast == 0 && a.lane_cells == 2u
                               ? (a.bf16 ? (const void*)k_persistent<true, true, 2>
                                         : (const void*)k_persistent<false, true, 2>)
                               : (a.bf16 ? (const void*)k_persistent<true, true>
                                         : (const void*)k_persistent<false, true>))
                        : (a.bf16 ? (const void*)k_persistent<true, false>
                                  : (const void*)k_persistent<false, false>);
-  const bool staged = !resident && general_one_barrier(a) && a.n_plast == 0 && a.lane_cells == 3u;
   const size_t smem = fused ? a.row_smem
                      : (a.seg_smem ? seg_smem_bytes(a) : 0) +
-                           ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0) +
-                           (staged ? kPairStageBlockBytes : 0);
+                           ((a.n_pull_units && a.pull_sum) ? pull_sum_bytes(a) : 0);
   return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(kPersistBlock), params, smem, s);
 }
 

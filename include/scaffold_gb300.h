@@ -175,7 +175,7 @@ typedef struct sgb_sim_info {
   int32_t deliver_blocks; /* per-step driver: blocks of the delivery kernel               */
   int32_t pull_summary;   /* dense pulls: 0 every entry reads its history word; 1 entries   */
                           /* settle on a staged spike summary; 2 as 1, the per-step pull  */
-                          /* also staging its entry stream in shared memory               */
+                          /* loading its entries 16 bytes at a time                       */
   int32_t spike_ahead;    /* SGB_KERNEL_FUSED: 1 the spike-ahead timeline (one substep)   */
   int32_t lane_cells;     /* SGB_KERNEL_GENERAL, one-barrier form: cells per lane (1, 2)  */
   int32_t reserved_;

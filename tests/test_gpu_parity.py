@@ -346,12 +346,8 @@ def test_general_kernel_block_item_overflow(delay):
     (sg.EXEC_PERSISTENT, sg.PROP_CSR, [7, 2, 1, 1]),  # fused, spike-ahead, 128-synapse items
     (sg.EXEC_PERSISTENT, sg.PROP_CSR, [6, 2, 1, 0]),  # fused, spikes in their own step
     (sg.EXEC_GRAPH, None, [6, 1, 0, 1]),              # per-step kernels: 1 delivery block per SM, no summary
-    (sg.EXEC_GRAPH, None, [6, 4, 1, 1]),              # k_pull with registers (summary, entries not staged)
-    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 2, 1]),       # k_pull_async: entry stream staged in shared memory
-    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 3, 0]),       # k_pull_vec: 16-byte entry loads
-    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 4, 0]),       # k_pull_q: passing entries queued, gathered
-    (sg.EXEC_GRAPH, None, [6, 2, 4, 0]),              # k_pull_q with pushes beside it
-    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 5, 0]),       # k_pull_q, 128-offset queues
+    (sg.EXEC_GRAPH, None, [6, 4, 1, 1]),              # k_pull: summary, four-byte entry loads
+    (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 2, 0]),       # k_pull_vec: 16-byte entry loads
     (sg.EXEC_PERSISTENT, sg.PROP_ELL, [6, 4, 0, 1]),  # resident kernel, pulls without the summary
 ])
 def test_cached_launch_shapes_bit_exact(tmp_path, exec_mode, prop, shape):
