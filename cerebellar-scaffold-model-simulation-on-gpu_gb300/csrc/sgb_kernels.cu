@@ -21,9 +21,9 @@
 // kernel comes in three forms: fused (every word resident in one warp, every
 // projection event-driven: update and push share one phase, one barrier a
 // step, push rows and items in shared memory; with one substep a step it
-// publishes each step's spikes one step early, as soon as the potential
-// that decides them is known, and reads every ring slot a step ahead of its
-// use), resident (words resident,
+// can also run a spike-ahead timeline, publishing each step's spikes one step
+// early, as soon as the potential that decides them is known, and reading
+// every ring slot a step ahead of its use), resident (words resident,
 // some dense pulls: two barriers) and general (more words than warps; one
 // barrier a step with the pushes in each block's shared memory when every
 // projection is event-driven, else two with a global item list).  With
@@ -2030,8 +2030,8 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// The fused kernel's forms: [BF16][timeline: 0 as read, 1..3 spike-ahead with
-// push items of 32, 64, 128 synapses].
+// The fused kernel's forms: [BF16][0: spikes in their own step, 64-synapse
+// items; 1..3: spike-ahead timeline with items of 32, 64, 128 synapses].
 static const void* const kFusedKernels[] = {
     (const void*)k_persistent_fused<false, false, 6>, (const void*)k_persistent_fused<false, true, 5>,
     (const void*)k_persistent_fused<false, true, 6>, (const void*)k_persistent_fused<false, true, 7>,
