@@ -1869,19 +1869,23 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       aborted = !grid_wait(a, target, s_poller);
     }
     for (uint32_t s = 0; s < n_steps && !aborted; ++s) {
-      // Ring slot t, fetched during the previous step: consumed and cleared.
+      StepIdx nx = ix;
+      nx.t = ix.t + 1ull;
+      nx.rel = s + 1u;
+      ix_advance(a, nx);
+      const bool more = s + 1u < n_steps;
+      // Ring slot t, fetched a step ago: consumed and cleared.  Slot t + 1 has
+      // been complete since the last grid barrier (every push into it was made
+      // a step earlier), so its copy goes out now and has the whole step to land.
       int2 acc = make_int2(0, 0);
       if (fetch) {
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncwarp();
         acc = s_acc[threadIdx.x];
         if (rd && (acc.x | acc.y)) __stcg(ring2 + (ix.roff + i), make_int2(0, 0));
+        __syncwarp();  // every lane has read its entry before the stage is refilled
+        if (more) fetch_slot(nx.roff);
       }
-      StepIdx nx = ix;
-      nx.t = ix.t + 1ull;
-      nx.rel = s + 1u;
-      ix_advance(a, nx);
-      const bool more = s + 1u < n_steps;
       const uint32_t par = (s + 1u) & 1u;
       // Shards of this step's spikes: their cells' bits in the history row of t.
       const bool sh_ck = threadIdx.x < n_sh;
@@ -1905,11 +1909,6 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
       deliver(par, ix.slot, shard_slot, sh_from);
       grid_arrive(a, target);
-      // Ring slot t + 1 has been complete since the previous grid barrier and
-      // nothing writes it before this warp clears it next step, so its copy is
-      // issued after the arrival (the release does not wait for it) and lands
-      // while the block waits at the barrier.
-      if (fetch && more) fetch_slot(ix.roff);
       if (stim && s + 2u < n_steps)
         in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
       if (!grid_wait(a, target, s_poller)) {
