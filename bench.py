@@ -383,7 +383,8 @@ def config4_leg(peak: float, bench_steps: int = 5, chunk: int = 1000):
 def ell_roofline(peak: float):
     """Dense ELL pull at HBM scale: config 5 (4 batched seeds of the ~925k-cell
     scaffold, 109M synapses, 437 MB of ELL entries, larger than L2) with every
-    projection forced to dense pull; k_pull time from CUDA events per launch.
+    projection forced to dense pull; the per-step pull kernel's time from CUDA
+    events per launch over 100 steps after a 1,000-step warm-up.
     Algorithmic bytes: 4 B per stored entry, plus W + 8 B per entry whose pre
     cell spiked (weight and ring atomic)."""
     import scaffold_gb300 as sg
@@ -395,8 +396,11 @@ def ell_roofline(peak: float):
     for k, net in enumerate(nets):
         for j in range(len(net.projections)):
             sim.set_propagation(k, j, sg.PROP_ELL)
-    sim.run(20)
-    mean_us, bytes_pl, nl = sim.profile(50)
+    # Past the start-up transient (every cell starts between reset and
+    # threshold, so many fire together in the first milliseconds), as the
+    # other legs are: 1,000 steps (0.1 s) before the timed launches.
+    sim.run(1000)
+    mean_us, bytes_pl, nl = sim.profile(100)
     info = sim.info()
     sim.close()
     gbs = bytes_pl[2] / (mean_us[2] * 1e-6) / 1e9
