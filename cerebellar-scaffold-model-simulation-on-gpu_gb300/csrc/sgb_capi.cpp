@@ -1,6 +1,7 @@
 // extern "C" entry points declared in include/scaffold_gb300.h.  Thin
 // argument checks and exception fences around the host model (sgb_model.cpp)
 // and the engine (sgb_engine.cu); no function here exits the process.
+#include <algorithm>
 #include <math.h>
 #include <string.h>
 
@@ -319,10 +320,10 @@ int sgb_sim_get_info(const sgb_sim* sim, sgb_sim_info* info) {
                           : SGB_KERNEL_GRAPH;
   info->push_smem_bytes = info->step_kernel == SGB_KERNEL_FUSED ? (int32_t)s.args.row_smem : 0;
   info->shard_cells = info->step_kernel == SGB_KERNEL_FUSED ? s.n_shard_cells : 0;
-  info->item_width = 1 << s.args.item_log2;
+  info->item_width = 1 << fused_item_log2(s.args);
   info->deliver_blocks = s.deliver_blocks;
   info->pull_summary = (int32_t)s.args.pull_sum;
-  info->spike_ahead = info->step_kernel == SGB_KERNEL_FUSED && s.cfg.substeps == 1 && s.args.ahead;
+  info->spike_ahead = info->step_kernel == SGB_KERNEL_FUSED ? (int32_t)fused_timeline(s.args) : 0;
   info->lane_cells = (int32_t)s.args.lane_cells;
   info->device_bytes = (int64_t)(s.ell_bytes + s.push_bytes + s.misc_bytes);
   info->exec_mode = s.cfg.exec_mode;

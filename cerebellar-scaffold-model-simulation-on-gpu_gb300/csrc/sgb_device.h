@@ -39,9 +39,9 @@ constexpr int kBlock = 256;           // threads per block of the per-step kerne
 constexpr int kPersistBlock = 1024;   // threads per block of the persistent kernel
 constexpr uint32_t kPushChunk = 256;  // synapses per push work item (8 per lane)
 // Fused persistent kernel: a cell with at least kShardMin synapses of delay
-// >= 2 keeps only its delay-1 synapses; the rest is cut into shards of
-// kPushChunk synapses that other blocks push one step later (at most
-// kMaxShards per block).
+// >= 3 keeps only its delay-1 and delay-2 synapses; the rest is cut into
+// shards of kPushChunk synapses that other blocks push one step later (two
+// in the late-push timeline; at most kMaxShards per block).
 constexpr uint32_t kShardMin = 256;
 constexpr uint32_t kMaxShards = 128;
 constexpr uint32_t kPullUnit = 1024;  // ELL entries per dense-pull work unit (32 per lane)
@@ -52,6 +52,14 @@ constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-m
 // Push-table synapse word: 27-bit padded post index, 4-bit delay, 1-bit accumulator.
 constexpr uint32_t kPushPostBits = 27;
 constexpr uint32_t kPushPostMask = (1u << kPushPostBits) - 1u;
+// Raster record: padded cell index (< 2^27) with the chunk-relative step mod 4
+// in bits 30-31.  The fused kernel's late-push timeline lets blocks run a step
+// apart, so a step's records may interleave with its neighbours'; the host
+// picks them out of the window between steps t - 2 and t + 2.
+constexpr uint32_t kRasterTagShift = 30;
+__host__ __device__ inline uint32_t raster_record(uint32_t cell, uint32_t rel) {
+  return cell | ((rel & 3u) << kRasterTagShift);
+}
 // Grid-barrier spin limit (iterations of ~64 ns sleeps): ~1 s, then the
 // kernel records kErrBarrierTimeout and returns.
 constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;  // grid-barrier wait limit (1 s)
@@ -179,9 +187,10 @@ struct StepArgs {
   uint32_t n_pad, n_words, n_segs, n_projs;
   uint32_t n_srcs;                // stimulus sources (all segments)
   uint32_t ring_slots, hist_rows;
-  uint32_t max_delay;             // longest synaptic delay, steps (ring_slots = max_delay + 2)
+  uint32_t max_delay;             // longest synaptic delay, steps (ring_slots = max_delay + 3)
   uint32_t item_log2;             // fused persistent kernel: push items of 2^item_log2 synapses
-  uint32_t ahead;                 // fused persistent kernel: spike-ahead timeline (one substep)
+  uint32_t ahead;                 // fused persistent kernel's timeline (one substep): 0 spikes in
+                                  // their own step, 1 late push, 2 late push, split barrier
   uint32_t lane_cells;            // general persistent kernel, one-barrier form: cells per lane (1, 2)
   uint32_t n_upd_words, n_pull_units;
   uint32_t n_plast, n_stdp_units;
@@ -232,6 +241,10 @@ size_t pull_sum_bytes(const StepArgs& a);  // shared memory of the staged summar
 size_t seg_smem_bytes(const StepArgs& a);  // shared memory of the segment descriptors
 // Which persistent kernel launch_persistent runs for these arguments (SGB_KERNEL_*).
 int persistent_kernel_kind(const StepArgs& a, int blocks);
-bool general_one_barrier(const StepArgs& a);  // the general kernel's one-barrier form applies
+bool general_one_barrier(const StepArgs& a);
+// The fused kernel's timeline (0 spikes in their own step, 1 late push, 2 late
+// push with a split barrier) and push-item width (log2) for these arguments.
+uint32_t fused_timeline(const StepArgs& a);
+uint32_t fused_item_log2(const StepArgs& a);  // the general kernel's one-barrier form applies
 
 }  // namespace sgb

@@ -209,19 +209,20 @@ static int upload_modes(Sim& s) {
   std::vector<uint32_t> syn((size_t)total);
   std::vector<float> wf(s.bf16 ? 0 : (size_t)total);
   std::vector<uint16_t> wh(s.bf16 ? (size_t)total : 0);
-  // Each row holds its delay-1 synapses first (pass 0), then the others:
-  // split[c] is where the delay >= 2 part of cell c's row starts.
+  // Each row holds its delay-1 synapses first (pass 0), then its delay-2
+  // synapses (pass 1), then the others: split[c] is where the delay >= 3 part
+  // of cell c's row starts.
   std::vector<uint32_t> split;
   {
     std::vector<uint32_t> fill(row.begin(), row.end() - 1);
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < 3; ++pass) {
       for (size_t k = 0; k < s.projs.size(); ++k) {
         if (s.projs[k].mode != SGB_PROP_CSR) continue;
         const ProjTables& t = s.ptab[k];
         const Projection& pr = s.nets[t.net].projs[t.proj];
         const uint32_t pre_base = s.segs[t.pre_seg].base, post_base = s.segs[t.post_seg].base;
         for (size_t i = 0; i < pr.pre_idx.size(); ++i) {
-          if ((pr.delay[i] == 1) != (pass == 0)) continue;
+          if (std::min<int>(pr.delay[i], 3) - 1 != pass) continue;
           const uint32_t q = fill[pre_base + pr.pre_idx[i]]++;
           syn[q] = (post_base + pr.post_idx[i]) | ((uint32_t)pr.delay[i] << kPushPostBits) |
                    ((uint32_t)pr.channel << 31);
@@ -229,7 +230,7 @@ static int upload_modes(Sim& s) {
           if (s.bf16) wh[q] = f32_to_bf16_bits(w); else wf[q] = w;
         }
       }
-      if (pass == 0) split = fill;
+      if (pass == 1) split = fill;
     }
   }
   const size_t wsz = s.bf16 ? 2 : 4;
@@ -255,12 +256,13 @@ static int upload_modes(Sim& s) {
     SGB_CUDA(cudaMemcpy((void*)a.pull_units, units.data(), units.size() * sizeof(PullUnit), cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMemcpy((void*)a.projs, s.projs.data(), s.projs.size() * sizeof(ProjDev), cudaMemcpyHostToDevice));
   a.n_pull_units = (uint32_t)units.size();
-  // Fused persistent kernel.  Shards: the delay >= 2 parts of long rows
+  // Fused persistent kernel.  Shards: the delay >= 3 parts of long rows
   // (longest first) are cut into kPushChunk-synapse shards dealt round-robin
   // over the blocks, so one spike's pushes spread over many SMs; a cell whose
   // shards no longer fit keeps its whole row.  Then shared memory for the
   // push rows of the block holding the most synapses (word slot ws runs in
-  // block ws mod blocks; a sharded cell's own part is its delay-1 synapses).
+  // block ws mod blocks; a sharded cell's own part is its delay-1 and delay-2
+  // synapses).
   a.row_smem = 0;
   a.n_shards = 0;
   s.n_shard_cells = 0;
@@ -421,12 +423,18 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     return set_error(SGB_ERR_UNSUPPORTED, "more than 2^27 cells (with padding) in one handle");
   s.n_words = s.n_pad / 32;
   s.n_cells = first_id;
-  // Ring slots t .. t + max_delay receive increments, plus one: the fused
+  // Ring slots t .. t + max_delay receive increments, plus two: the fused
   // kernel's spike-ahead timeline reads slot t + 1 during step t and clears
-  // it during step t + 1, while pushes target slots up to t + 1 + max_delay.
+  // it during step t + 1, while pushes target slots up to t + 1 + max_delay;
+  // its late-push timeline fences step t's clear of slot t only with the
+  // barrier arrival at the top of step t + 1, so the clear is ordered before
+  // the pushes of step t + 2 and later only.
   s.max_delay = (uint32_t)max_delay;
-  s.ring_slots = (uint32_t)max_delay + 2;
-  s.hist_rows = (uint32_t)max_delay;
+  s.ring_slots = (uint32_t)max_delay + 3;
+  // History rows: one per delay; at least 4 where delays reach 3 (shards are
+  // then possible): in the fused kernel's late-push timeline a block may
+  // rewrite a row up to one step before a block behind it reads that row.
+  s.hist_rows = (uint32_t)(max_delay >= 3 ? std::max(max_delay, 4) : max_delay);
   // A plastic synapse with delay d reads its pre cell's spikes d .. d +
   // window - 1 steps back, a teacher up to max_delay steps back.  Windows that
   // end within 64 steps come from the per-cell spike registers instead.
@@ -645,8 +653,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.substeps = cfg.substeps;
   a.bar_extra = (uint32_t)cfg.barrier_test_extra;
   s.deliver_blocks = 2 * s.sm_count;
-  a.item_log2 = 6;  // push items of 64 synapses (the autotuner may pick 32 or 128)
-  a.ahead = 0;      // fused kernel: spikes in their own step (the autotuner may pick spike-ahead)
+  a.item_log2 = 6;  // push items of 64 synapses (the autotuner may pick 128)
+  a.ahead = 1;      // fused kernel, one substep: late push (the autotuner may pick another timeline)
   a.lane_cells = 2;  // general kernel, one-barrier form: two cells per lane (or one: autotuner)
   // Dense pulls settle entries on the staged summary where it fits; the
   // per-step pull kernel may also stage its entry stream (the autotuner's
@@ -965,15 +973,21 @@ int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int
           SGB_CUDA(cudaMemcpyAsync(s.h_raster, a.raster, (size_t)nrec * 4, cudaMemcpyDeviceToHost, s.stream));
           SGB_CUDA(cudaStreamSynchronize(s.stream));
         }
+        // Step r's records lie after every record of step r - 2 and before
+        // every record of step r + 2 (blocks run at most a step apart), and
+        // carry r mod 4.
         for (uint32_t r = 0; r < c; ++r) {
-          const uint32_t b = s.h_raster_off[r], e = s.h_raster_off[r + 1];
+          const uint32_t b = s.h_raster_off[r > 0 ? r - 1 : 0];
+          const uint32_t e = std::min<uint32_t>(s.h_raster_off[std::min(r + 2, c)], s.raster_cap);
+          const uint32_t need = s.h_raster_off[r + 1] - s.h_raster_off[r];
           const int64_t start = rfill;
-          for (uint32_t q = b; q < e; ++q) {
-            if (q >= s.raster_cap || rfill >= raster_cap) {
+          for (uint32_t q = b; q < e && rfill - start < (int64_t)need; ++q) {
+            if ((s.h_raster[q] >> kRasterTagShift) != (r & 3u)) continue;
+            if (rfill >= raster_cap) {
               overflow = true;
               break;
             }
-            const uint32_t pid = s.h_raster[q];
+            const uint32_t pid = s.h_raster[q] & ((1u << kRasterTagShift) - 1u);
             // Segment of the padded id by binary search over segment bases.
             size_t lo = 0, hi = nseg;
             while (hi - lo > 1) {
@@ -982,6 +996,7 @@ int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int
             }
             raster_ids[rfill++] = (uint32_t)(s.seg_first_id[lo] + (pid - s.segs[lo].base));
           }
+          if (rfill - start < (int64_t)need) overflow = true;  // records past a capacity
           std::sort(raster_ids + start, raster_ids + rfill);
           raster_offsets[done + r + 1] = rfill;
         }
@@ -1149,10 +1164,11 @@ static std::string tune_signature(const Sim& s) {
 
 // Launch shapes the autotuner picks beside the modes and the driver.
 struct TuneShape {
-  int32_t item_log2;     // fused kernel: push items of 2^item_log2 synapses
+  int32_t item_log2;     // fused kernel: push items of 2^item_log2 synapses (6 or 7)
   int32_t deliver_mult;  // per-step driver: delivery blocks per SM
   int32_t pull_sum;      // dense pulls: 0 no summary, 1 staged summary, 2 also 16-byte entry loads
-  int32_t ahead;         // fused kernel: 1 spike-ahead timeline, 0 spikes in their own step
+  int32_t ahead;         // fused kernel's timeline: 0 spikes in their own step, 1 late push,
+                         // 2 late push with a split barrier
   int32_t lane_cells;    // general kernel's one-barrier form: cells per lane (1 or 2)
 };
 
@@ -1164,11 +1180,11 @@ static TuneShape current_shape(const Sim& s) {
 // Applies a shape (kept within what the handle supports); captured graphs
 // hold the old kernel arguments and are dropped.
 static void apply_shape(Sim& s, const TuneShape& t) {
-  s.args.item_log2 = (uint32_t)std::min(7, std::max(5, t.item_log2));
+  s.args.item_log2 = (uint32_t)std::min(7, std::max(6, t.item_log2));
   s.deliver_blocks = std::min(8, std::max(1, t.deliver_mult)) * s.sm_count;
   const bool ok = t.pull_sum == 0 || (s.pull_sum_fits && t.pull_sum >= 1 && t.pull_sum <= 2);
   s.args.pull_sum = ok ? (uint32_t)t.pull_sum : (s.pull_sum_fits ? 2u : 0u);
-  s.args.ahead = t.ahead ? 1u : 0u;
+  s.args.ahead = (uint32_t)std::min(2, std::max(0, t.ahead));
   s.args.lane_cells = t.lane_cells >= 2 ? 2u : 1u;
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
@@ -1321,16 +1337,19 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   for (auto& kv : s.graphs) cudaGraphExecDestroy(kv.second);
   s.graphs.clear();
   // Launch shapes for the chosen driver and modes, one dimension at a time:
-  // the fused kernel's push-item width, the per-step delivery grid, and
-  // whether dense pulls settle entries on a staged spike summary.
+  // the fused kernel's timeline and push-item width, the general kernel's
+  // cells per lane, the per-step delivery grid, and the dense-pull variant.
   {
     TuneShape cur = current_shape(s);
     std::vector<TuneShape> cands;
     const bool persistent = s.cfg.exec_mode == SGB_EXEC_PERSISTENT;
     if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_FUSED &&
         s.cfg.substeps == 1) {
-      for (int32_t w : {5, 7}) cands.push_back({w, cur.deliver_mult, cur.pull_sum, 1, cur.lane_cells});
-      cands.push_back({6, cur.deliver_mult, cur.pull_sum, 0, cur.lane_cells});  // the other timeline
+      // The three timelines; the two late-push ones with each item width.
+      for (int32_t tl = 0; tl <= 2; ++tl)
+        for (int32_t w = 6; w <= (tl ? 7 : 6); ++w)
+          if (tl != cur.ahead || w != cur.item_log2)
+            cands.push_back({w, cur.deliver_mult, cur.pull_sum, tl, cur.lane_cells});
     }
     if (persistent && persistent_kernel_kind(s.args, s.persistent_blocks) == SGB_KERNEL_GENERAL &&
         general_one_barrier(s.args) && s.args.n_plast == 0)

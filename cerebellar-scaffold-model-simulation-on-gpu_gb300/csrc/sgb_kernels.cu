@@ -21,9 +21,10 @@
 // kernel comes in three forms: fused (every word resident in one warp, every
 // projection event-driven: update and push share one phase, one barrier a
 // step, push rows and items in shared memory; with one substep a step it
-// can also run a spike-ahead timeline, publishing each step's spikes one step
-// early, as soon as the potential that decides them is known, and reading
-// every ring slot a step ahead of its use), resident (words resident,
+// publishes each step's spikes one step early, as soon as the potential that
+// decides them is known, and makes a step's writes after its barrier
+// arrival -- the late-push timeline, optionally with a split barrier),
+// resident (words resident,
 // some dense pulls: two barriers) and general (more words than warps; one
 // barrier a step with the pushes in each block's shared memory when every
 // projection is event-driven, else two with a global item list).  With
@@ -289,7 +290,7 @@ __device__ __forceinline__ uint32_t publish_word(const StepArgs& a, uint32_t w, 
     roff = __shfl_sync(kFull, roff, 0);
     if (fired) {
       if (roff + rank < a.raster_cap)
-        a.raster[roff + rank] = i;
+        a.raster[roff + rank] = raster_record(i, ix.rel);
       else
         atomicOr(&ctl->error, kErrRasterOverflow);
     }
@@ -526,11 +527,13 @@ __device__ __forceinline__ uint32_t publish_pair(const StepArgs& a, uint32_t p, 
     roff = __shfl_sync(kFull, roff, 0) + rincl - rk;
     uint32_t q = roff;
     if (f0) {
-      if (q < a.raster_cap) a.raster[q] = c; else atomicOr(&ctl->error, kErrRasterOverflow);
+      if (q < a.raster_cap) a.raster[q] = raster_record(c, ix.rel);
+      else atomicOr(&ctl->error, kErrRasterOverflow);
       ++q;
     }
     if (f1) {
-      if (q < a.raster_cap) a.raster[q] = c + 1u; else atomicOr(&ctl->error, kErrRasterOverflow);
+      if (q < a.raster_cap) a.raster[q] = raster_record(c + 1u, ix.rel);
+      else atomicOr(&ctl->error, kErrRasterOverflow);
     }
   }
   return walked;
@@ -1218,30 +1221,47 @@ __device__ __forceinline__ void grid_arrive(const StepArgs& a, unsigned long lon
     asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
 }
 
+// One thread polls the arrival counter until it reaches target (plus the
+// tests' a.bar_extra) with gpu-scope acquire loads, for at most
+// kBarrierTimeoutNs of global time; false (and kErrBarrierTimeout recorded)
+// when the wait ran out or another block had already recorded a timeout.
+__device__ __forceinline__ bool poll_arrivals(const StepArgs& a, unsigned long long target) {
+  const unsigned long long want = target + a.bar_extra;
+  unsigned long long t0 = 0;
+  uint32_t it = 0;
+  while (ld_acquire(a.bar) < want) {
+    if ((++it & 255u) == 0u) {
+      const unsigned long long now = global_ns();
+      if (t0 == 0) t0 = now;
+      if (now - t0 > kBarrierTimeoutNs || (__ldcg(&a.ctl->error) & kErrBarrierTimeout)) {
+        atomicOr(&a.ctl->error, kErrBarrierTimeout);
+        return false;
+      }
+    }
+    __nanosleep(32);
+  }
+  return true;
+}
+
 __device__ __forceinline__ bool grid_wait(const StepArgs& a, unsigned long long target,
                                           uint32_t poller = 0) {
   __shared__ int abort_flag;
-  if (threadIdx.x == poller) {
-    int ok = 1;
-    const unsigned long long want = target + a.bar_extra;
-    unsigned long long t0 = 0;
-    uint32_t it = 0;
-    while (ld_acquire(a.bar) < want) {
-      if ((++it & 255u) == 0u) {
-        const unsigned long long now = global_ns();
-        if (t0 == 0) t0 = now;
-        if (now - t0 > kBarrierTimeoutNs || (__ldcg(&a.ctl->error) & kErrBarrierTimeout)) {
-          atomicOr(&a.ctl->error, kErrBarrierTimeout);
-          ok = 0;
-          break;
-        }
-      }
-      __nanosleep(32);
-    }
-    abort_flag = !ok;
-  }
+  if (threadIdx.x == poller) abort_flag = !poll_arrivals(a, target);
   __syncthreads();
   return !abort_flag;
+}
+
+// Arrival by one thread whose gpu-scope fence comes first: the fence followed
+// by the relaxed reduction is a release pattern, cumulative over the writes
+// that a block barrier ordered before the fence.
+__device__ __forceinline__ void grid_arrive_fenced(const StepArgs& a) {
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
+}
+
+// Block barrier 1 over the first n threads (a multiple of 32).
+__device__ __forceinline__ void bar_sync_first(uint32_t n) {
+  asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory");
 }
 
 __device__ __forceinline__ bool grid_barrier(const StepArgs& a, unsigned long long& target) {
@@ -1522,9 +1542,10 @@ __device__ __forceinline__ uint32_t push_any(const StepArgs& a, const uint2* row
   return (it.y & 1u) ? push_item_smem(a, rows, it, s0) : push_item<BF16>(a, it, s0);
 }
 
-// AHEAD: the spike-ahead timeline of one-substep steps (see the loop below).
+// TL: the step's timeline -- 0 spikes in their own step; for one-substep steps
+// 1 late push, 2 late push with a split grid barrier (see the loops below).
 // ILOG: push items of 2^ILOG synapses.
-template <bool BF16, bool AHEAD, uint32_t ILOG>
+template <bool BF16, uint32_t TL, uint32_t ILOG>
 __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs a,
                                                                        uint32_t n_steps) {
   __shared__ uint2 s_items[kBlockItems];
@@ -1578,11 +1599,12 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       r1 = __ldg(a.push_row + i + 1);
     }
   }
-  // Shards: a sharded cell pushes only its delay-1 synapses (r1 becomes its
-  // split point); the rest of its row is cut into shards dealt to blocks,
-  // which push a shard in the step after the cell's spike, reading the spike
-  // from the history.  Its delays d >= 2 count from the spike's ring slot, so
-  // the targets t - 1 + d are still ahead of the update that reads slot t.
+  // Shards: a sharded cell pushes only its delay-1 and delay-2 synapses (r1
+  // becomes its split point); the rest of its row is cut into shards dealt to
+  // blocks, which push a shard in the step after the cell's spike (two steps
+  // after it in the late-push timeline), reading the spike from the history.
+  // Its delays d >= 3 count from the spike's ring slot, so the targets are
+  // still ahead of the updates that read them.
   // This block's n_sh shards go first into shared memory while they fit.
   const bool sharded = a.n_shards != 0 && gridDim.x == a.shard_grid;
   uint32_t n_sh = 0;
@@ -1720,7 +1742,7 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       roff = __shfl_sync(kFull, roff, 0);
       if (fired) {
         if (roff + rank < a.raster_cap)
-          a.raster[roff + rank] = i;
+          a.raster[roff + rank] = raster_record(i, rel);
         else
           atomicOr(&ctl->error, kErrRasterOverflow);
       }
@@ -1747,12 +1769,15 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
   // The block's items of parity par, then the items past the list's
   // capacity; own rows count their delays from ring slot `own`, shards from
   // ring slot `shard` (their spike's step).
-  auto deliver = [&](uint32_t par, uint32_t own, uint32_t shard, uint32_t sh_from) {
-    __syncthreads();
+  // nw: the warps that deliver (the first nw of the block; fewer than all of
+  // them meet on block barrier 1 instead of 0).
+  auto deliver = [&](uint32_t par, uint32_t own, uint32_t shard, uint32_t sh_from,
+                     uint32_t nw = kPersistBlock / 32) {
+    if (nw == kPersistBlock / 32) __syncthreads(); else bar_sync_first(nw * 32u);
     const uint32_t n_items = min(s_n[par], kBlockItems);
-    // The other parity's count was last read before this __syncthreads.
+    // The other parity's count was last read before this block barrier.
     if (threadIdx.x == 0) s_n[par ^ 1u] = 0;
-    for (uint32_t u = wib; u < n_items; u += kPersistBlock / 32)
+    for (uint32_t u = wib; u < n_items; u += nw)
       walked += push_any<BF16>(a, s_rows, s_items[u], own, shard);
     uint32_t spill = __ballot_sync(kFull, off + nit > kBlockItems);
     while (spill) {
@@ -1780,7 +1805,24 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       }
     }
   };
-  if (!AHEAD) {
+  // The shards of the spikes of step ix.t - 1 (ix has advanced past that
+  // step): the epilogue of the timelines that push shards a step late.
+  auto last_shards = [&]() {
+    const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
+    bool hit = false;
+    if (threadIdx.x < n_sh) {
+      const uint32_t c = s_sh[threadIdx.x].x;
+      hit = (__ldcg(hist_base(a, ix.hrow) + a.n_words + (c >> 5)) >> (c & 31u)) & 1u;
+    }
+    uint32_t sp = __ballot_sync(kFull, hit);
+    while (sp) {
+      const int src = __ffs(sp) - 1;
+      sp &= sp - 1;
+      const uint4 h = s_sh[wib * 32u + src];
+      walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
+    }
+  };
+  if (TL == 0) {
     // Step t: update (ring slot t), spikes of t, their pushes and the shards
     // of step t - 1's spikes; one grid barrier.
     for (uint32_t s = 0; s < n_steps; ++s) {
@@ -1810,54 +1852,30 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       ix_advance(a, ix);
     }
     // The shards of the last step's spikes (ix has advanced past that step).
-    if (!aborted && n_sh && n_steps) {
-      const uint32_t prev = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
-      bool hit = false;
-      if (threadIdx.x < n_sh) {
-        const uint32_t c = s_sh[threadIdx.x].x;
-        hit = (__ldcg(hist_base(a, ix.hrow) + a.n_words + (c >> 5)) >> (c & 31u)) & 1u;
-      }
-      uint32_t sp = __ballot_sync(kFull, hit);
-      while (sp) {
-        const int src = __ffs(sp) - 1;
-        sp &= sp - 1;
-        const uint4 h = s_sh[wib * 32u + src];
-        walked += push_any<BF16>(a, s_rows, make_uint2(h.y, h.z), ix.slot, prev);
-      }
-    }
-  } else {
-    // Spike-ahead timeline (one substep per step).  A cell's spike of step
-    // t + 1 is decided by its potential after the update of step t (the spike
-    // test reads the potential before the step's integration), so step t
-    // updates with ring slot t, then publishes and pushes the spikes of
-    // t + 1 and the shards of t's spikes.  Every push into ring slot t + 1 is
-    // then made by the end of step t - 1, so the slot is read at the start of
-    // step t, a whole step ahead of its use: the step's critical path has no
-    // ring read.  A prologue publishes and pushes the spikes of the launch's
-    // first step; the last step publishes nothing and leaves its next slot
-    // unread, so a launch ends in the same state as with the other timeline.
-    // The ring slot a LIF word consumes next is staged in shared memory by
-    // asynchronous 16-byte copies at L2 (cp.async.cg: never a stale L1 line),
-    // so no registers are held for it across the pushes and the barrier.  The
-    // slot is cleared at the start of the step that consumes it: with
-    // max_delay + 2 ring slots no push of that step targets it, and the
-    // clears' acknowledgements return during the update, not at the
-    // barrier's release.
-    __shared__ __align__(16) int2 s_acc[kPersistBlock];
+    if (!aborted && n_sh && n_steps) last_shards();
+  } else if (TL == 1) {
+    // Late-push timeline (one substep per step).  A cell's spike of step t + 1
+    // is decided by its potential after the update of step t (the spike test
+    // reads the potential before the step's integration), so step t updates
+    // with ring slot t and publishes the spikes of t + 1, whose pushes target
+    // slots t + 2 and later.  Those pushes are first read after the barrier of
+    // step t + 1, so a block arrives at step t's barrier as soon as its cells
+    // are updated, and only then makes the step's writes -- the clears of the
+    // slot it consumed, the history words, counts and pushes of the new
+    // spikes, the shards of step t - 1's spikes (delays >= 3) -- while the
+    // other blocks arrive: the next arrival's release carries them.
+    //   Slot t + 1 is complete at step t + 1's start: own pushes into it come
+    // from steps <= t - 1, shards from steps <= t - 1 as well (a shard reads
+    // the spike of step T in the history row written in step T - 1 and pushes
+    // in step T + 1).  A clear made after step t's arrival is ordered before
+    // the pushes of step t + 2 and later only; with max_delay + 3 ring slots
+    // no push of step t + 1 targets slot t again.  A prologue publishes and
+    // pushes the spikes of the launch's first step; the last step publishes
+    // nothing, so a launch ends in the same state as with the other timelines.
     int2* ring2 = reinterpret_cast<int2*>(a.ring);
     const bool rd = has && lif && valid;
-    const bool fetch = has && lif;  // warp-uniform
-    auto fetch_slot = [&](uint32_t roff) {  // lanes 0..15: two cells each
-      if (lane < 16u) {
-        const int2* src = ring2 + (roff + (w << 5) + 2u * lane);
-        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_acc[(wib << 5) + 2u * lane]);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
     bool in_next = false;  // input spike of step t + 1, drawn a step ahead
     if (n_steps) {
-      if (fetch) fetch_slot(ix.roff);
       if (stim && n_steps > 1)
         in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), t0 + 1);
       ix.rel = 0;
@@ -1869,34 +1887,24 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
       aborted = !grid_wait(a, target, s_poller);
     }
     for (uint32_t s = 0; s < n_steps && !aborted; ++s) {
-      StepIdx nx = ix;
-      nx.t = ix.t + 1ull;
-      nx.rel = s + 1u;
-      ix_advance(a, nx);
       const bool more = s + 1u < n_steps;
-      // Ring slot t, fetched a step ago: consumed and cleared.  Slot t + 1 has
-      // been complete since the last grid barrier (every push into it was made
-      // a step earlier), so its copy goes out now and has the whole step to land.
       int2 acc = make_int2(0, 0);
-      if (fetch) {
-        asm volatile("cp.async.wait_all;" ::: "memory");
-        __syncwarp();
-        acc = s_acc[threadIdx.x];
-        if (rd && (acc.x | acc.y)) __stcg(ring2 + (ix.roff + i), make_int2(0, 0));
-        __syncwarp();  // every lane has read its entry before the stage is refilled
-        if (more) fetch_slot(nx.roff);
-      }
-      const uint32_t par = (s + 1u) & 1u;
-      // Shards of this step's spikes: their cells' bits in the history row of t.
-      const bool sh_ck = threadIdx.x < n_sh;
-      const uint32_t sh_w = sh_ck ? __ldcg(hist_base(a, ix.hrow) + (s_sh[threadIdx.x].x >> 5)) : 0u;
-      const uint32_t shard_slot = ix.slot;
-      ix = nx;  // from here on: step t + 1, whose spikes this step publishes
+      if (rd) acc = __ldcg(ring2 + (ix.roff + i));
+      const uint32_t consumed = ix.roff;
+      // Shards of step t - 1's spikes (none at a launch's first step: the
+      // previous launch pushed them after its loop).
+      const bool sh_ck = s > 0 && threadIdx.x < n_sh;
+      const uint32_t sh_w =
+          sh_ck ? __ldcg(hist_base(a, ix.hrow) + a.n_words + (s_sh[threadIdx.x].x >> 5)) : 0u;
+      const uint32_t shard_slot = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
+      // From here on ix is step t + 1, whose spikes this step publishes.
+      ix.t += 1ull;
+      ix.rel = s + 1u;
+      ix_advance(a, ix);
       clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x,
                          gridDim.x * kPersistBlock);  // the row of step t + 2
-      off = nit = 0;
+      bool fired = false;
       if (has) {
-        bool fired = false;
         if (lif) {
           const LifK k = lif_k(segs[seg]);
           if (rd) lif_update<1>(k, 1, st, acc);
@@ -1904,11 +1912,14 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         } else {
           fired = in_next;
         }
-        if (more) publish(fired, ix, s + 1u, par);
       }
+      grid_arrive(a, target);
+      if (rd && (acc.x | acc.y)) __stcg(ring2 + (consumed + i), make_int2(0, 0));
+      const uint32_t par = (s + 1u) & 1u;
+      off = nit = 0;
+      if (has && more) publish(fired, ix, s + 1u, par);
       const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
       deliver(par, ix.slot, shard_slot, sh_from);
-      grid_arrive(a, target);
       if (stim && s + 2u < n_steps)
         in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
       if (!grid_wait(a, target, s_poller)) {
@@ -1916,6 +1927,107 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         break;
       }
     }
+    // The shards of the last step's spikes (ix has advanced past that step).
+    if (!aborted && n_sh && n_steps) last_shards();
+  } else {
+    // Late-push timeline with a split grid barrier (one substep per step).
+    // The steps' work and data as in the timeline above, but every write of
+    // step t is first read in step t + 2, so the barrier is split: at the top
+    // of step t + 1, after the block barrier that ends step t, warp 31 fences
+    // the block's writes of step t and arrives; the block waits for the other
+    // blocks' arrivals only at the end of step t + 1, before step t + 2 reads
+    // slot t + 2.  Arrival, fence and barrier latency overlap a step's work,
+    // and blocks run at most one step apart, which adds to the timeline above:
+    //   * a history row is rewritten hist_rows steps later: with shards the
+    //     handle keeps at least 4 rows, so that no block rewrites a row before
+    //     a block one step behind has read it for its shards;
+    //   * warp 31 clears the summary row of step t + 2 at the top of step t,
+    //     before its fence; its bits are set in step t + 1;
+    //   * the raster records of neighbouring steps may interleave (each
+    //     record carries its step mod 4).
+    // A warp 31 without a word of its own polls right after arriving while
+    // the other 31 warps work (they meet on block barrier 1); one with a word
+    // works like the others and the block's poller polls at the end.
+    int2* ring2 = reinterpret_cast<int2*>(a.ring);
+    const bool rd = has && lif && valid;
+    const bool sync_idle = 31u * gridDim.x + blockIdx.x >= a.n_upd_words;  // block-uniform
+    const uint32_t nw = sync_idle ? kPersistBlock / 32 - 1u : kPersistBlock / 32;
+    __shared__ int s_ok[2];
+    bool in_next = false;  // input spike of step t + 1, drawn a step ahead
+    if (n_steps) {
+      // Prologue: the spikes of the launch's first step, published and pushed
+      // (fenced with the first arrival, read from step t0 + 1 on).
+      if (stim && n_steps > 1)
+        in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), t0 + 1);
+      ix.rel = 0;
+      clear_next_summary(a, ix, blockIdx.x * kPersistBlock + threadIdx.x, gridDim.x * kPersistBlock);
+      off = nit = 0;
+      if (has) publish(valid && (lif ? st.x > segs[seg].Vth : next_in), ix, 0u, 0u);
+      deliver(0u, ix.slot, ix.slot, kNoRow);
+      __syncthreads();
+    }
+    for (uint32_t s = 0; s < n_steps; ++s) {
+      const bool more = s + 1u < n_steps;
+      target += gridDim.x;
+      if (wib == 31u) {
+        const uint32_t row = (ix.srow + 2u) % (a.hist_rows + 1u);  // summary row of step t + 2
+        for (uint32_t j = blockIdx.x * 32u + lane; j < a.n_swords; j += gridDim.x * 32u)
+          __stcg(a.hsum + (size_t)row * a.n_swords + j, 0u);
+        __syncwarp();
+        if (lane == 0) {
+          grid_arrive_fenced(a);
+          if (sync_idle) s_ok[s & 1u] = poll_arrivals(a, target);
+        }
+        __syncwarp();
+      }
+      if (!sync_idle || wib != 31u) {
+        int2 acc = make_int2(0, 0);
+        if (rd) acc = __ldcg(ring2 + (ix.roff + i));
+        const uint32_t consumed = ix.roff;
+        // Shards of step t - 1's spikes (none at a launch's first step: the
+        // previous launch pushed them after its loop).
+        const bool sh_ck = s > 0 && threadIdx.x < n_sh;
+        const uint32_t sh_w =
+            sh_ck ? __ldcg(hist_base(a, ix.hrow) + a.n_words + (s_sh[threadIdx.x].x >> 5)) : 0u;
+        const uint32_t shard_slot = ix.slot == 0u ? a.ring_slots - 1u : ix.slot - 1u;
+        // From here on ix is step t + 1, whose spikes this step publishes.
+        ix.t += 1ull;
+        ix.rel = s + 1u;
+        ix_advance(a, ix);
+        bool fired = false;
+        if (has) {
+          if (lif) {
+            const LifK k = lif_k(segs[seg]);
+            if (rd) lif_update<1>(k, 1, st, acc);
+            fired = valid && st.x > k.Vth;
+          } else {
+            fired = in_next;
+            // The next draw while the LIF warps wait for their ring reads.
+            if (stim && s + 2u < n_steps)
+              in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x),
+                                   ix.t + 1ull);
+          }
+        }
+        if (rd && (acc.x | acc.y)) __stcg(ring2 + (consumed + i), make_int2(0, 0));
+        const uint32_t par = (s + 1u) & 1u;
+        off = nit = 0;
+        if (has && more) publish(fired, ix, s + 1u, par);
+        const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
+        deliver(par, ix.slot, shard_slot, sh_from, nw);
+        if (!sync_idle && threadIdx.x == s_poller) s_ok[s & 1u] = poll_arrivals(a, target);
+      } else {
+        ix.t += 1ull;
+        ix.rel = s + 1u;
+        ix_advance(a, ix);
+      }
+      __syncthreads();  // ends the step: the next arrival fences its writes
+      if (!s_ok[s & 1u]) {
+        aborted = true;
+        break;
+      }
+    }
+    // The shards of the last step's spikes (ix has advanced past that step).
+    if (!aborted && n_sh && n_steps) last_shards();
   }
   if (valid && lif) state_out(a, i, st);
   if (a.raster_cap && blockIdx.x == 0) raster_offsets_from_counts(a, n_steps, s_wsum);
@@ -2030,17 +2142,26 @@ cudaError_t launch_chunk_end(const StepArgs& a, cudaStream_t s) {
 }
 
 // The fused kernel's forms: [BF16][0: spikes in their own step, 64-synapse
-// items; 1..3: spike-ahead timeline with items of 32, 64, 128 synapses].
-static const void* const kFusedKernels[] = {
-    (const void*)k_persistent_fused<false, false, 6>, (const void*)k_persistent_fused<false, true, 5>,
-    (const void*)k_persistent_fused<false, true, 6>, (const void*)k_persistent_fused<false, true, 7>,
-    (const void*)k_persistent_fused<true, false, 6>, (const void*)k_persistent_fused<true, true, 5>,
-    (const void*)k_persistent_fused<true, true, 6>, (const void*)k_persistent_fused<true, true, 7>};
+// items; 1, 2: late-push timeline, 3, 4: late push with the split barrier,
+// each with items of 64 and 128 synapses].
+#define SGB_FUSED_FORMS(B)                                                                  \
+  (const void*)k_persistent_fused<B, 0, 6>, (const void*)k_persistent_fused<B, 1, 6>,        \
+      (const void*)k_persistent_fused<B, 1, 7>, (const void*)k_persistent_fused<B, 2, 6>,    \
+      (const void*)k_persistent_fused<B, 2, 7>
+constexpr uint32_t kFusedForms = 5;
+static const void* const kFusedKernels[] = {SGB_FUSED_FORMS(false), SGB_FUSED_FORMS(true)};
+#undef SGB_FUSED_FORMS
+
+// The timeline and item width the fused kernel runs with for these arguments.
+uint32_t fused_timeline(const StepArgs& a) { return a.substeps == 1 ? std::min(a.ahead, 2u) : 0u; }
+uint32_t fused_item_log2(const StepArgs& a) {
+  return fused_timeline(a) ? (a.item_log2 >= 7 ? 7u : 6u) : 6u;
+}
 
 static const void* fused_kernel(const StepArgs& a) {
-  const uint32_t form =
-      a.substeps == 1 && a.ahead ? std::min(7u, std::max(5u, a.item_log2)) - 4u : 0u;
-  return kFusedKernels[(a.bf16 ? 4u : 0u) + form];
+  const uint32_t tl = fused_timeline(a);
+  const uint32_t form = tl ? 2u * tl - 1u + (fused_item_log2(a) - 6u) : 0u;
+  return kFusedKernels[(a.bf16 ? kFusedForms : 0u) + form];
 }
 
 static int fused_blocks_per_sm() {

@@ -169,14 +169,16 @@ typedef struct sgb_sim_info {
   int64_t pulled;        /* dense-pull entries whose pre cell had spiked (deliveries) since the last reset */
   int64_t pull_entries;  /* dense-table entries streamed per step (0 without dense projections) */
   int64_t l2_persist_bytes; /* L2 set aside for the persisting state window (0: none)   */
-  int64_t shard_cells;   /* SGB_KERNEL_FUSED: cells whose delay >= 2 synapses other blocks push */
+  int64_t shard_cells;   /* SGB_KERNEL_FUSED: cells whose delay >= 3 synapses other blocks push */
   /* Launch shapes (defaults, or the autotuner's choice): */
   int32_t item_width;     /* SGB_KERNEL_FUSED: synapses per push item (32, 64 or 128)      */
   int32_t deliver_blocks; /* per-step driver: blocks of the delivery kernel               */
   int32_t pull_summary;   /* dense pulls: 0 every entry reads its history word; 1 entries   */
                           /* settle on a staged spike summary; 2 as 1, the per-step pull  */
                           /* loading its entries 16 bytes at a time                       */
-  int32_t spike_ahead;    /* SGB_KERNEL_FUSED: 1 the spike-ahead timeline (one substep)   */
+  int32_t spike_ahead;    /* SGB_KERNEL_FUSED, one substep: the step's timeline; 0 spikes  */
+                          /* in their own step, 1 spike-ahead, 2 spike-ahead with the     */
+                          /* pushes made after the barrier arrival (late push)            */
   int32_t lane_cells;     /* SGB_KERNEL_GENERAL, one-barrier form: cells per lane (1, 2)  */
   int32_t reserved_;
 } sgb_sim_info;

@@ -255,7 +255,7 @@ def test_fused_kernel_rows_partly_in_shared_memory(weight):
     info = sim.info()
     assert info.step_kernel == 3  # SGB_KERNEL_FUSED
     assert 0 < info.push_smem_bytes < 32000 * 8
-    assert info.shard_cells > 0   # ~750 synapses of delay >= 2 per cell
+    assert info.shard_cells > 0   # ~500 synapses of delay >= 3 per cell
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 5, steps, bf16=weight == sg.WEIGHT_BF16)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
@@ -266,9 +266,10 @@ def test_fused_kernel_rows_partly_in_shared_memory(weight):
 @pytest.mark.parametrize("chunk", [97, 1000])
 def test_config2_fused_shards_bit_exact(chunk):
     """Config 2 (92,550 cells) in the fused persistent kernel: the Golgi cells'
-    1,600-synapse rows keep their delay-1 synapses and hand the rest, as
-    256-synapse shards, to other blocks one step later; short chunks check
-    that every launch pushes its last step's shards before it ends."""
+    1,600-synapse rows keep their delay-1 and delay-2 synapses and hand the
+    rest, as 256-synapse shards, to other blocks a step or two later; short
+    chunks check that every launch pushes its last step's shards before it
+    ends."""
     net = sg.scaffold(2, 1.0, 3)
     steps = 400
     sim = sg.Simulation([net], [3], exec_mode=sg.EXEC_PERSISTENT, raster=True, chunk_steps=chunk)
@@ -281,12 +282,12 @@ def test_config2_fused_shards_bit_exact(chunk):
     sim.close()
 
 
-@pytest.mark.parametrize("delay", [1, 2])
+@pytest.mark.parametrize("delay", [1, 2, 3])
 def test_fused_kernel_item_list_overflow(delay):
     """Every one of 4,864 input cells fires every step with 5,000 synapses:
-    with delay 1 each block's own push items exceed its shared-memory list
-    (the overflow is pushed by the warps that made it); with delay 2 the rows
-    are sharded until the shard capacity runs out and the shards' items
+    with delay 1 or 2 each block's own push items exceed its shared-memory
+    list (the overflow is pushed by the warps that made it); with delay 3 the
+    rows are sharded until the shard capacity runs out and the shards' items
     overflow the list too.  Bit-exact against the oracle."""
     rng = np.random.default_rng(23)
     net = sg.Network()
@@ -302,7 +303,7 @@ def test_fused_kernel_item_list_overflow(delay):
     steps = 40
     sim = sg.Simulation([net], [9], exec_mode=sg.EXEC_PERSISTENT, raster=True, chunk_steps=20)
     assert sim.info().step_kernel == 3  # SGB_KERNEL_FUSED
-    if delay == 2:
+    if delay == 3:
         assert 0 < sim.info().shard_cells < 4864
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 9, steps, raster_cap=1 << 20)
@@ -342,9 +343,11 @@ def test_general_kernel_block_item_overflow(delay):
 
 
 @pytest.mark.parametrize("exec_mode,prop,shape", [
-    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [5, 2, 1, 1]),  # fused, spike-ahead, 32-synapse items
-    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [7, 2, 1, 1]),  # fused, spike-ahead, 128-synapse items
     (sg.EXEC_PERSISTENT, sg.PROP_CSR, [6, 2, 1, 0]),  # fused, spikes in their own step
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [6, 2, 1, 1]),  # fused, late push, 64-synapse items
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [7, 2, 1, 1]),  # fused, late push, 128-synapse items
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [6, 2, 1, 2]),  # fused, late push, split barrier
+    (sg.EXEC_PERSISTENT, sg.PROP_CSR, [7, 2, 1, 2]),  # the same, 128-synapse items
     (sg.EXEC_GRAPH, None, [6, 1, 0, 1]),              # per-step kernels: 1 delivery block per SM, no summary
     (sg.EXEC_GRAPH, None, [6, 4, 1, 1]),              # k_pull: summary, four-byte entry loads
     (sg.EXEC_GRAPH, sg.PROP_ELL, [6, 2, 2, 0]),       # k_pull_vec: 16-byte entry loads
