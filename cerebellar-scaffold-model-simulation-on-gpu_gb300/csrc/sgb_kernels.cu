@@ -1872,8 +1872,15 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
     // no push of step t + 1 targets slot t again.  A prologue publishes and
     // pushes the spikes of the launch's first step; the last step publishes
     // nothing, so a launch ends in the same state as with the other timelines.
+    //   A warp 31 without a word of its own arrives and polls while the other
+    // 31 warps make the step's writes (they meet on block barrier 1), so the
+    // arrival's release stalls no warp with work; otherwise thread 0 arrives
+    // and the block's poller polls after the writes.
     int2* ring2 = reinterpret_cast<int2*>(a.ring);
     const bool rd = has && lif && valid;
+    const bool sync_idle = 31u * gridDim.x + blockIdx.x >= a.n_upd_words;  // block-uniform
+    const uint32_t nw = sync_idle ? kPersistBlock / 32 - 1u : kPersistBlock / 32;
+    __shared__ int s_ok1[2];
     bool in_next = false;  // input spike of step t + 1, drawn a step ahead
     if (n_steps) {
       if (stim && n_steps > 1)
@@ -1913,16 +1920,29 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
           fired = in_next;
         }
       }
-      grid_arrive(a, target);
-      if (rd && (acc.x | acc.y)) __stcg(ring2 + (consumed + i), make_int2(0, 0));
-      const uint32_t par = (s + 1u) & 1u;
-      off = nit = 0;
-      if (has && more) publish(fired, ix, s + 1u, par);
-      const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
-      deliver(par, ix.slot, shard_slot, sh_from);
-      if (stim && s + 2u < n_steps)
-        in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
-      if (!grid_wait(a, target, s_poller)) {
+      __syncthreads();  // the block's updates (and the previous step's writes) are done
+      target += gridDim.x;
+      if (sync_idle && wib == 31u) {
+        if (lane == 0) {
+          asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
+          s_ok1[s & 1u] = poll_arrivals(a, target);
+        }
+        __syncwarp();
+      } else {
+        if (!sync_idle && threadIdx.x == 0)
+          asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(a.bar) : "memory");
+        if (rd && (acc.x | acc.y)) __stcg(ring2 + (consumed + i), make_int2(0, 0));
+        const uint32_t par = (s + 1u) & 1u;
+        off = nit = 0;
+        if (has && more) publish(fired, ix, s + 1u, par);
+        const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
+        deliver(par, ix.slot, shard_slot, sh_from, nw);
+        if (stim && s + 2u < n_steps)
+          in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
+        if (!sync_idle && threadIdx.x == s_poller) s_ok1[s & 1u] = poll_arrivals(a, target);
+      }
+      __syncthreads();
+      if (!s_ok1[s & 1u]) {
         aborted = true;
         break;
       }
