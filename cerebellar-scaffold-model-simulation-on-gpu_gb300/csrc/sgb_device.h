@@ -52,10 +52,11 @@ constexpr uint32_t kEllColMajorMaxK = 48;  // widths up to this use the column-m
 // Push-table synapse word: 27-bit padded post index, 4-bit delay, 1-bit accumulator.
 constexpr uint32_t kPushPostBits = 27;
 constexpr uint32_t kPushPostMask = (1u << kPushPostBits) - 1u;
-// Raster record: padded cell index (< 2^27) with the chunk-relative step mod 4
-// in bits 30-31.  The fused kernel's late-push timeline lets blocks run a step
-// apart, so a step's records may interleave with its neighbours'; the host
-// picks them out of the window between steps t - 2 and t + 2.
+// Raster record of the fused kernel: padded cell index (< 2^27) with the
+// chunk-relative step mod 4 in bits 30-31.  Its late-push timelines let blocks
+// run a step apart, so a step's records may interleave with its neighbours';
+// the host picks them out of the window between steps t - 2 and t + 2.  The
+// other kernels write the bare index, their steps' records in step order.
 constexpr uint32_t kRasterTagShift = 30;
 __host__ __device__ inline uint32_t raster_record(uint32_t cell, uint32_t rel) {
   return cell | ((rel & 3u) << kRasterTagShift);

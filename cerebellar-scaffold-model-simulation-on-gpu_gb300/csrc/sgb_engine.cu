@@ -423,18 +423,22 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
     return set_error(SGB_ERR_UNSUPPORTED, "more than 2^27 cells (with padding) in one handle");
   s.n_words = s.n_pad / 32;
   s.n_cells = first_id;
-  // Ring slots t .. t + max_delay receive increments, plus two: the fused
-  // kernel's spike-ahead timeline reads slot t + 1 during step t and clears
-  // it during step t + 1, while pushes target slots up to t + 1 + max_delay;
-  // its late-push timeline fences step t's clear of slot t only with the
-  // barrier arrival at the top of step t + 1, so the clear is ordered before
-  // the pushes of step t + 2 and later only.
+  // Ring slots t .. t + max_delay receive increments.  Networks that may run
+  // the fused kernel (at most one 32-cell word per warp of the persistent
+  // grid) keep two more: its late-push timelines clear slot t after step t's
+  // barrier arrival, so the clear is ordered only before the pushes of step
+  // t + 2 and later, while step t + 1 pushes up to slot t + 2 + max_delay.
+  // The others keep one more (the layout their kernels were measured with).
   s.max_delay = (uint32_t)max_delay;
-  s.ring_slots = (uint32_t)max_delay + 3;
-  // History rows: one per delay; at least 4 where delays reach 3 (shards are
-  // then possible): in the fused kernel's late-push timeline a block may
+  uint64_t upd_words_n = 0;
+  for (const SegDev& d : s.segs) upd_words_n += (d.count + 31u) / 32u;
+  const bool may_fuse = upd_words_n * 32u <=
+                        (uint64_t)std::max(1, cfg.blocks_per_sm) * s.sm_count * kPersistBlock;
+  s.ring_slots = (uint32_t)max_delay + (may_fuse ? 3u : 2u);
+  // History rows: one per delay; where the fused kernel may run with shards
+  // (delays >= 3) at least 4: in its split-barrier timeline a block may
   // rewrite a row up to one step before a block behind it reads that row.
-  s.hist_rows = (uint32_t)(max_delay >= 3 ? std::max(max_delay, 4) : max_delay);
+  s.hist_rows = (uint32_t)(may_fuse && max_delay >= 3 ? std::max(max_delay, 4) : max_delay);
   // A plastic synapse with delay d reads its pre cell's spikes d .. d +
   // window - 1 steps back, a teacher up to max_delay steps back.  Windows that
   // end within 64 steps come from the per-cell spike registers instead.
@@ -973,16 +977,21 @@ int sim_run(Sim& s, int64_t n_steps, uint32_t* counts, uint32_t* raster_ids, int
           SGB_CUDA(cudaMemcpyAsync(s.h_raster, a.raster, (size_t)nrec * 4, cudaMemcpyDeviceToHost, s.stream));
           SGB_CUDA(cudaStreamSynchronize(s.stream));
         }
-        // Step r's records lie after every record of step r - 2 and before
-        // every record of step r + 2 (blocks run at most a step apart), and
-        // carry r mod 4.
+        // Records are in step order, except from the fused kernel's late-push
+        // timelines: there step r's records lie after every record of step
+        // r - 2 and before every record of step r + 2 (blocks run at most a
+        // step apart), and carry r mod 4.
+        const bool windowed = s.cfg.exec_mode == SGB_EXEC_PERSISTENT &&
+                              persistent_kernel_kind(a, s.persistent_blocks) == SGB_KERNEL_FUSED &&
+                              fused_timeline(a) != 0;
         for (uint32_t r = 0; r < c; ++r) {
-          const uint32_t b = s.h_raster_off[r > 0 ? r - 1 : 0];
-          const uint32_t e = std::min<uint32_t>(s.h_raster_off[std::min(r + 2, c)], s.raster_cap);
+          const uint32_t b = s.h_raster_off[windowed && r > 0 ? r - 1 : r];
+          const uint32_t e = std::min<uint32_t>(s.h_raster_off[windowed ? std::min(r + 2, c) : r + 1],
+                                                s.raster_cap);
           const uint32_t need = s.h_raster_off[r + 1] - s.h_raster_off[r];
           const int64_t start = rfill;
           for (uint32_t q = b; q < e && rfill - start < (int64_t)need; ++q) {
-            if ((s.h_raster[q] >> kRasterTagShift) != (r & 3u)) continue;
+            if (windowed && (s.h_raster[q] >> kRasterTagShift) != (r & 3u)) continue;
             if (rfill >= raster_cap) {
               overflow = true;
               break;

@@ -290,7 +290,7 @@ __device__ __forceinline__ uint32_t publish_word(const StepArgs& a, uint32_t w, 
     roff = __shfl_sync(kFull, roff, 0);
     if (fired) {
       if (roff + rank < a.raster_cap)
-        a.raster[roff + rank] = raster_record(i, ix.rel);
+        a.raster[roff + rank] = i;
       else
         atomicOr(&ctl->error, kErrRasterOverflow);
     }
@@ -527,13 +527,11 @@ __device__ __forceinline__ uint32_t publish_pair(const StepArgs& a, uint32_t p, 
     roff = __shfl_sync(kFull, roff, 0) + rincl - rk;
     uint32_t q = roff;
     if (f0) {
-      if (q < a.raster_cap) a.raster[q] = raster_record(c, ix.rel);
-      else atomicOr(&ctl->error, kErrRasterOverflow);
+      if (q < a.raster_cap) a.raster[q] = c; else atomicOr(&ctl->error, kErrRasterOverflow);
       ++q;
     }
     if (f1) {
-      if (q < a.raster_cap) a.raster[q] = raster_record(c + 1u, ix.rel);
-      else atomicOr(&ctl->error, kErrRasterOverflow);
+      if (q < a.raster_cap) a.raster[q] = c + 1u; else atomicOr(&ctl->error, kErrRasterOverflow);
     }
   }
   return walked;
