@@ -592,9 +592,9 @@ def run_gb300(a):
     if kname in ("k_persistent_fused", "k_persistent_resident"):
         # Resident networks live in L2: the step is bounded by its chain of L2
         # round trips and the grid barrier, not by HBM bandwidth.
-        roof["limiter"] = ("latency: L2-resident network; per 0.1-ms step a ring-slot read, the "
-                           "release of the block's reductions and the grid barrier are dependent "
-                           "L2 round trips")
+        roof["limiter"] = ("latency: L2-resident network; per 0.1-ms step the ring-slot read, the "
+                           "cell update and the grid barrier's arrival and propagation are "
+                           "dependent L2 round trips (the step's pushes overlap the barrier)")
     # Per-phase view from an instrumented run of the per-step kernels (CUDA
     # events on the handle's stream around every launch).
     mean_us, bytes_pl, nl = sim.profile(1000)
