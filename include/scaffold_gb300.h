@@ -176,9 +176,11 @@ typedef struct sgb_sim_info {
   int32_t pull_summary;   /* dense pulls: 0 every entry reads its history word; 1 entries   */
                           /* settle on a staged spike summary; 2 as 1, the per-step pull  */
                           /* loading its entries 16 bytes at a time                       */
-  int32_t spike_ahead;    /* SGB_KERNEL_FUSED, one substep: the step's timeline; 0 spikes  */
-                          /* in their own step, 1 spike-ahead, 2 spike-ahead with the     */
-                          /* pushes made after the barrier arrival (late push)            */
+  int32_t spike_ahead;    /* SGB_KERNEL_FUSED: the step's timeline; 0 spikes in their own  */
+                          /* step (always with substeps > 1); 1 late push: a step         */
+                          /* publishes the next step's spikes and makes its writes after  */
+                          /* its grid-barrier arrival; 2 late push with the barrier split */
+                          /* across steps                                                 */
   int32_t lane_cells;     /* SGB_KERNEL_GENERAL, one-barrier form: cells per lane (1, 2)  */
   int32_t reserved_;
 } sgb_sim_info;
