@@ -21,7 +21,8 @@
 //              double-buffered by step parity.  The fused persistent kernel
 //              keeps its items, and its blocks' push rows, in shared memory.
 //   push table one cell-major CSR over every projection in event-driven mode
-//              (all instances), each row's delay-1 synapses first: synapse
+//              (all instances), each row's delay-1 synapses first, then its
+//              delay-2 synapses, then the rest: synapse
 //              word = padded post index | delay << 27 | accumulator << 31, plus
 //              the weight pre-multiplied by its accumulator's 2^S (exact
 //              power-of-two scaling) in FP32 or BF16.
