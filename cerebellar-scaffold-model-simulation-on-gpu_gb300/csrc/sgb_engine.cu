@@ -657,8 +657,8 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   a.substeps = cfg.substeps;
   a.bar_extra = (uint32_t)cfg.barrier_test_extra;
   s.deliver_blocks = 2 * s.sm_count;
-  a.item_log2 = 6;  // push items of 64 synapses (the autotuner may pick 128)
-  a.ahead = 1;      // fused kernel, one substep: late push (set below from the grid's size)
+  a.item_log2 = 7;  // fused kernel's late-push timelines: push items of 128 synapses (or 64)
+  a.ahead = 2;      // fused kernel, one substep: late push with the split barrier (or another)
   a.lane_cells = 2;  // general kernel, one-barrier form: two cells per lane (or one: autotuner)
   // Dense pulls settle entries on the staged summary where it fits; the
   // per-step pull kernel may also stage its entry stream (the autotuner's
@@ -778,12 +778,6 @@ int sim_create(const sgb_config& cfg, sgb_net* const* nets, const uint64_t* seed
   const int bpsm = std::min(cfg.blocks_per_sm > 0 ? cfg.blocks_per_sm : 1,
                             persistent_blocks_per_sm(s.bf16));
   s.persistent_blocks = std::max(1, bpsm) * s.sm_count;
-  // Fused kernel, one substep: with few words per block (<= 8) a step is the
-  // grid barrier's latency, which the split barrier overlaps with the work;
-  // with more, a block's own work is as long as the barrier and the plain
-  // late-push timeline is faster (config 1 / config 2 scaffolds: 1.72 / 2.46 us
-  // per step with the choice made here).
-  a.ahead = upd_words.size() <= (size_t)8 * s.persistent_blocks ? 2u : 1u;
 
   SGB_CUDA(cudaMemcpy((void*)a.segs, s.segs.data(), nseg * sizeof(SegDev), cudaMemcpyHostToDevice));
   SGB_CUDA(cudaMallocHost(&s.h_srcs, std::max<size_t>(s.srcs.size(), 1) * sizeof(SrcDev)));

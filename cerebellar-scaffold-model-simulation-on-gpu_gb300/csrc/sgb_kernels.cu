@@ -2020,10 +2020,6 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
             fired = valid && st.x > k.Vth;
           } else {
             fired = in_next;
-            // The next draw while the LIF warps wait for their ring reads.
-            if (stim && s + 2u < n_steps)
-              in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x),
-                                   ix.t + 1ull);
           }
         }
         if (rd && (acc.x | acc.y)) __stcg(ring2 + (consumed + i), make_int2(0, 0));
@@ -2032,6 +2028,8 @@ __global__ void __launch_bounds__(kPersistBlock, 1) k_persistent_fused(StepArgs 
         if (has && more) publish(fired, ix, s + 1u, par);
         const uint32_t sh_from = shard_items(sh_ck, sh_w, par);
         deliver(par, ix.slot, shard_slot, sh_from, nw);
+        if (stim && s + 2u < n_steps)
+          in_next = input_fire(a, srcs, segs[seg], __float_as_uint(st.y), __float_as_uint(st.x), ix.t + 1ull);
         if (!sync_idle && threadIdx.x == s_poller) s_ok[s & 1u] = poll_arrivals(a, target);
       } else {
         ix.t += 1ull;

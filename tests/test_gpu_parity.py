@@ -47,8 +47,9 @@ def test_c1_quarter_bit_exact(prop, weight, exec_mode):
     sim = sg.Simulation([net], [11], weight_type=weight, exec_mode=exec_mode, default_prop=prop,
                         raster=True, chunk_steps=500)
     if exec_mode == sg.EXEC_PERSISTENT and prop == sg.PROP_CSR:
-        # few words per block: the fused kernel's split-barrier timeline by default
+        # the fused kernel's split-barrier timeline by default, 128-synapse items
         assert sim.info().step_kernel == 3 and sim.info().spike_ahead == 2
+        assert sim.info().item_width == 128
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 11, steps, bf16=weight == sg.WEIGHT_BF16)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
@@ -278,7 +279,7 @@ def test_config2_fused_shards_bit_exact(chunk):
     sim = sg.Simulation([net], [3], exec_mode=sg.EXEC_PERSISTENT, raster=True, chunk_steps=chunk)
     info = sim.info()
     assert info.step_kernel == 3 and info.shard_cells >= 200
-    assert info.spike_ahead == 1  # ~19 words per block: the late-push timeline by default
+    assert info.spike_ahead == 2  # the split-barrier timeline by default
     counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
     exp = _oracle(net, 3, steps)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
