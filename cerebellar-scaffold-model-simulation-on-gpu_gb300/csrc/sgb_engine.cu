@@ -1111,6 +1111,72 @@ int sim_totals(Sim& s, double* totals) {
   return SGB_OK;
 }
 
+// A change of propagation modes at a step boundary (step T about to run).
+// A projection's spikes of steps S < T reach their targets' ring slots S + d
+// either pushed in (or before) step S, or pulled in step S + d - 1: at the
+// boundary, a projection that pushed has already delivered its recent
+// spikes' contributions to slots T + 1 and later, which its pulls would add
+// again, and one that pulled has not yet delivered them.  So for every
+// projection whose mode changed, each synapse of delay d >= 2 whose pre cell
+// spiked in step S = T - k (k = 1 .. d - 1; from the spike history) has its
+// fixed-point increment taken out of slot S + d (push -> pull) or added to it
+// (pull -> push).  The ring holds integer sums, so the run continues exactly
+// as if the new modes had been in place from the start.
+static int handover_modes(Sim& s, const std::vector<uint32_t>& before) {
+  std::vector<size_t> changed;
+  for (size_t k = 0; k < s.projs.size(); ++k)
+    if (before[k] != s.projs[k].mode) changed.push_back(k);
+  if (changed.empty() || s.max_delay < 2) return SGB_OK;
+  SGB_CUDA(cudaStreamSynchronize(s.stream));
+  Ctl ctl;
+  SGB_CUDA(cudaMemcpy(&ctl, s.args.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  const uint64_t T = ctl.step;
+  if (T == 0) return SGB_OK;
+  const uint32_t H = s.hist_rows, R = s.ring_slots, D = s.max_delay;
+  std::vector<uint32_t> hist((size_t)2 * H * s.n_words);
+  SGB_CUDA(cudaMemcpy(hist.data(), s.args.hist, hist.size() * 4, cudaMemcpyDeviceToHost));
+  // Row of step T - k: the rows run in decreasing step order from that of T
+  // (the second copy covers the wrap).
+  auto spiked = [&](uint32_t k, uint32_t cell) {
+    const size_t row = (size_t)(H - 1u - ctl.hist_row + k) * s.n_words;
+    return (hist[row + (cell >> 5)] >> (cell & 31u)) & 1u;
+  };
+  // Ring slots T + 1 .. T + D - 1.
+  std::vector<int2> slots((size_t)(D - 1) * s.n_pad);
+  auto slot_of = [&](uint32_t ahead) { return (ctl.ring_slot + ahead) % R; };
+  for (uint32_t j = 1; j < D; ++j)
+    SGB_CUDA(cudaMemcpy(slots.data() + (size_t)(j - 1) * s.n_pad,
+                        (const int2*)s.args.ring + (size_t)slot_of(j) * s.n_pad,
+                        (size_t)s.n_pad * 8, cudaMemcpyDeviceToHost));
+  for (size_t k : changed) {
+    const ProjTables& t = s.ptab[k];
+    const Projection& pr = s.nets[t.net].projs[t.proj];
+    const uint32_t pre_base = s.segs[t.pre_seg].base, post_base = s.segs[t.post_seg].base;
+    const int32_t sign = s.projs[k].mode == SGB_PROP_ELL ? -1 : 1;
+    for (size_t i = 0; i < pr.pre_idx.size(); ++i) {
+      const uint32_t d = pr.delay[i];
+      const uint32_t pre = pre_base + pr.pre_idx[i];
+      for (uint32_t back = 1; back < d && back <= T; ++back) {
+        if (!spiked(back, pre)) continue;
+        const int32_t inc = (int32_t)lrintf(scaled_weight(pr.weight[i], t.scale_bits, s.bf16));
+        int2& e = slots[(size_t)(d - back - 1) * s.n_pad + post_base + pr.post_idx[i]];
+        (pr.channel ? e.y : e.x) += sign * inc;
+      }
+    }
+  }
+  for (uint32_t j = 1; j < D; ++j)
+    SGB_CUDA(cudaMemcpy((int2*)s.args.ring + (size_t)slot_of(j) * s.n_pad,
+                        slots.data() + (size_t)(j - 1) * s.n_pad, (size_t)s.n_pad * 8,
+                        cudaMemcpyHostToDevice));
+  return SGB_OK;
+}
+
+static std::vector<uint32_t> current_modes(const Sim& s) {
+  std::vector<uint32_t> m(s.projs.size());
+  for (size_t k = 0; k < m.size(); ++k) m[k] = s.projs[k].mode;
+  return m;
+}
+
 int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
   if (net < 0 || net >= (int32_t)s.nets.size()) return set_error(SGB_ERR_ARG, "net %d out of range", net);
   if (proj < 0 || proj >= (int32_t)s.nets[net].projs.size())
@@ -1118,8 +1184,10 @@ int sim_set_mode(Sim& s, int32_t net, int32_t proj, int32_t mode) {
   if (mode != SGB_PROP_CSR && mode != SGB_PROP_ELL) return set_error(SGB_ERR_ARG, "mode must be CSR or ELL");
   if (s.nets[net].projs[proj].plastic && mode != SGB_PROP_ELL)
     return set_error(SGB_ERR_UNSUPPORTED, "projection %d is plastic: it stays in dense pull", proj);
+  const std::vector<uint32_t> before = current_modes(s);
   s.projs[s.net_proj0[net] + proj].mode = (uint32_t)mode;
-  return upload_modes(s);
+  int rc = upload_modes(s);
+  return rc ? rc : handover_modes(s, before);
 }
 
 int sim_set_stream(Sim& s, cudaStream_t st) {
@@ -1262,11 +1330,13 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
   std::vector<int32_t> modes;
   int32_t exec_mode = s.cfg.exec_mode;
   TuneShape shape = current_shape(s);
+  const std::vector<uint32_t> modes0 = current_modes(s);
   if (tune_cache_read(cache_path, sig, &exec_mode, modes, &shape) &&
       modes.size() == s.projs.size()) {
     s.cfg.exec_mode = exec_mode;
     apply_shape(s, shape);
-    return apply_modes(s, modes);
+    int rc = apply_modes(s, modes);
+    return rc ? rc : handover_modes(s, modes0);
   }
   // Snapshot of the device state a run changes.
   const StepArgs& a = s.args;
@@ -1384,6 +1454,9 @@ int sim_autotune(Sim& s, int32_t n_steps, const char* cache_path) {
     shape = cur;
   }
   if (save(true)) return fail(set_error(SGB_ERR_CUDA, "autotune restore failed"));
+  // The restored state carries the deliveries in flight under the modes the
+  // handle had before tuning.
+  if ((rc = handover_modes(s, modes0))) return fail(rc);
   tune_cache_write(cache_path, sig, s.cfg.exec_mode, modes, shape, best);
   return fail(SGB_OK);
 }

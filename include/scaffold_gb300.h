@@ -373,7 +373,12 @@ int sgb_sim_write_raster(const sgb_sim* sim, const char* path, const uint32_t* i
  * device at the end of every chunk). */
 int sgb_sim_spike_totals(sgb_sim* sim, double* totals);
 
-/* Propagation mode of projection `proj` of net `net` (SGB_PROP_CSR/ELL). */
+/* Propagation mode of projection `proj` of net `net` (SGB_PROP_CSR/ELL), from
+ * the next step on.  Any time between runs: the contributions of the last
+ * (max delay - 1) steps' spikes still on their way are handed over (taken back
+ * out of the ring when the projection starts pulling, added when it starts
+ * pushing), so the run continues bit for bit as if the new mode had been in
+ * place from the start; the autotuner does the same with its choice. */
 int sgb_sim_set_propagation(sgb_sim* sim, int32_t net, int32_t proj, int32_t mode);
 int sgb_sim_get_propagation(const sgb_sim* sim, int32_t net, int32_t proj, int32_t* mode);
 

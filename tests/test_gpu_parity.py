@@ -392,3 +392,54 @@ def test_cached_launch_shapes_bit_exact(tmp_path, exec_mode, prop, shape):
     exp = _oracle(net, 3, steps)
     _assert_same(sim, (counts, ids, offs), sim.state(), exp)
     sim.close()
+
+
+@pytest.mark.parametrize("shape", [None, [6, 2, 1, 1], [6, 2, 1, 0]])
+def test_fused_timelines_hand_over_to_dense_pulls(tmp_path, shape):
+    """Every fused-kernel timeline ends a launch in the state the other kernels
+    expect: full config 1 runs 700 steps all event-driven (fused kernel;
+    default timeline, late push, or spikes in their own step), then every
+    other projection pulls densely for 600 steps (the resident kernel reads
+    the spike history and summary rows the fused launches left), then all
+    push again for 300 steps.  Counts, rasters and the final state against
+    one 1,600-step oracle run."""
+    import json
+
+    net = sg.scaffold(1, 1.0, 5)
+    n = len(net.projections)
+    kw = dict(raster=True, chunk_steps=250, exec_mode=sg.EXEC_PERSISTENT,
+              default_prop=sg.PROP_CSR)
+    if shape is None:
+        sim = sg.Simulation([net], [5], **kw)
+    else:
+        cache = str(tmp_path / "tune.jsonl")
+        first = sg.Simulation([net], [5], chunk_steps=250, exec_mode=sg.EXEC_PERSISTENT)
+        first.autotune(20, cache)
+        first.close()
+        line = json.loads(open(cache).read().splitlines()[0])
+        line.update(exec_mode=sg.EXEC_PERSISTENT, modes=[sg.PROP_CSR] * n, shape=shape)
+        with open(cache, "w") as f:
+            f.write(json.dumps(line) + "\n")
+        sim = sg.Simulation([net], [5], **kw)
+        sim.autotune(20, cache)
+    assert sim.info().step_kernel == 3
+    assert sim.info().spike_ahead == (2 if shape is None else shape[3])
+    exp = _oracle(net, 5, 1600)
+    ecounts, eids, eoffs = exp[0], exp[1], exp[2]
+    s0 = 0
+    for steps, ell in ((700, False), (600, True), (300, False)):
+        for j in range(n):
+            sim.set_propagation(0, j, sg.PROP_ELL if ell and j % 2 else sg.PROP_CSR)
+        assert sim.info().step_kernel == (2 if ell else 3)
+        counts, (ids, offs) = sim.loop_n_steps(steps, raster=True)
+        s1 = s0 + steps
+        bad = np.nonzero((counts != ecounts[s0:s1]).any(1))[0]
+        assert bad.size == 0, f"segment from step {s0}: first divergent step {s0 + bad[0]}"
+        assert np.array_equal(offs, eoffs[s0:s1 + 1] - eoffs[s0])
+        assert np.array_equal(ids, eids[eoffs[s0]:eoffs[s1]])
+        s0 = s1
+    u, g, ref = sim.state()
+    assert np.array_equal(u.view(np.uint32), exp[3].view(np.uint32))
+    assert np.array_equal(g.view(np.uint32), exp[4].view(np.uint32))
+    assert np.array_equal(ref, exp[5])
+    sim.close()
