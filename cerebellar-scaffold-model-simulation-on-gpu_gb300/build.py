@@ -7,7 +7,9 @@ Usage: python build.py [--force]
 from __future__ import annotations
 
 import concurrent.futures as cf
+import json
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -49,13 +51,14 @@ def _newer(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def _compile(src: str, kind: str) -> str:
+def _compile(src: str, kind: str) -> tuple[str, bool]:
+    """Object of one translation unit, and whether it was compiled now."""
     path = os.path.join(CSRC, src)
     obj = os.path.join(BUILD, src + ".o")
     deps = [path] + [os.path.join(CSRC, h) for h in HEADERS] + [
         os.path.join(INCLUDE, "scaffold_gb300.h"), os.path.join(INCLUDE, "scaffold_compat.h")]
     if not _newer(obj, deps):
-        return obj
+        return obj, False
     if kind == "cxx":
         cmd = [CXX] + HOST_FLAGS + ["-I", os.path.join(CUDA_HOME, "include"), "-c", path, "-o", obj]
     else:
@@ -63,22 +66,34 @@ def _compile(src: str, kind: str) -> str:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-    return obj
+    return obj, True
 
 
 def build(force: bool = False) -> str:
+    """Builds the library if any source is newer than it; writes what was done
+    (units compiled or up to date, whether the library was linked) to
+    _build/build_record.json and prints it as one JSON line."""
     os.makedirs(BUILD, exist_ok=True)
     if force:
         for f in os.listdir(BUILD):
             if f.endswith(".o"):
                 os.remove(os.path.join(BUILD, f))
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(*s), SOURCES))
-    if force or _newer(LIB, objs):
+        done = list(ex.map(lambda s: _compile(*s), SOURCES))
+    objs = [o for o, _ in done]
+    linked = force or _newer(LIB, objs)
+    if linked:
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    record = {"lib": LIB, "arch": ARCH[1],
+              "compiled": [src for (src, _), (_, c) in zip(SOURCES, done) if c],
+              "up_to_date": [src for (src, _), (_, c) in zip(SOURCES, done) if not c],
+              "linked": linked, "machine": platform.machine()}
+    with open(os.path.join(BUILD, "build_record.json"), "w") as f:
+        json.dump(record, f)
+    print("build record: " + json.dumps(record), flush=True)
     return LIB
 
 
