@@ -1205,7 +1205,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // __syncthreads), then polls with gpu-scope acquire loads; the closing
 // __syncthreads hands the acquired view to the whole block.  No separate
 // fences: measured on 152 blocks, ~0.3 us per barrier less than fence +
-// atomicAdd + fence.  It waits for all blocks of this round (plus
+// atomicAdd + fence.  It waits for every block's arrival at this barrier (plus
 // a.bar_extra arrivals that no block makes, in the tests of this limit) -- at
 // most kBarrierTimeoutNs of global time, checked every 256 polls.  On timeout it records
 // kErrBarrierTimeout; every block then returns at its next barrier (or as
